@@ -1,0 +1,231 @@
+/*
+ * tfcuda.h -- C ABI of libtfcuda.so, the GB300 (sm_103a) backend of the
+ * TransiFlow finite-volume hot path.
+ *
+ * Conventions
+ *   - Every device buffer is allocated by the caller (the Python host layer
+ *     uses PyTorch's caching allocator).  Functions never allocate or free;
+ *     scratch needs are reported by *_workspace_bytes queries.
+ *   - Pointers named d_* are device pointers; everything else is host memory.
+ *   - All work is enqueued on the given stream (0 = legacy default stream)
+ *     and is stream ordered; functions return before the GPU finishes.
+ *   - Return value: TF_OK (0) or a positive TF_ERR_* code; tf_error_string()
+ *     describes it.  Non-convergence of an iterative method is reported
+ *     through output arguments, never by a trap.
+ *   - State vectors are interleaved per cell, [u, v, (w), p, (T)] with x
+ *     fastest: index = d + dof * (i + nx * (j + ny * k)), as in
+ *     transiflow/utils.py:23-60 (create_state_mtx).
+ *
+ * Reference interfaces replaced (BIMAU/transiflow 1.0.1):
+ *   tf_assemble         Discretization.rhs / jacobian, Discretization.py:367-415
+ *                       (+ nonlinear_part :319-365, linear_part :210-317,
+ *                       boundaries :704-714, assemble_rhs :439-472,
+ *                       assemble_jacobian :474-524)
+ *   tf_stencil_pattern  the column structure of assemble_jacobian, :507-522
+ *   tf_csr_compact      CrsMatrix.compress, CrsMatrix.py:52-71
+ *   tf_mass_diag        Discretization.mass_matrix, Discretization.py:417-548
+ *   tf_gauge_values     SciPy.Interface.compute_bordered_matrix pressure fix,
+ *                       interface/SciPy.py:93-103
+ *   tf_spmv_*           scipy CSC @ and CrsMatrix.matvec, CrsMatrix.py:155-170
+ *   tf_nd_*             splu / lu.solve, interface/SciPy.py:151, 194-202
+ *   tf_vec_*            vector algebra used by Continuation.py and by the
+ *                       GMRES that replaces scipy.sparse.linalg.gmres
+ */
+#ifndef TFCUDA_H
+#define TFCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *tf_stream_t;
+
+enum {
+    TF_OK = 0,
+    TF_ERR_ARG = 1,          /* invalid argument (null pointer, bad size)   */
+    TF_ERR_UNSUPPORTED = 2,  /* (dim, dof) combination not compiled in      */
+    TF_ERR_CUDA = 3,         /* a CUDA launch or runtime call failed        */
+    TF_ERR_SIZE = 4          /* a size exceeds a compiled-in maximum        */
+};
+
+/* ---- problem description -------------------------------------------------*/
+
+#define TF_MAX_BC_OPS 24
+
+enum { TF_BC_WALL = 1, TF_BC_FORCE = 2 };
+
+/* One boundary-condition primitive applied to the atoms of the cells on one
+ * face of the box (BoundaryConditions.py:55-544):
+ *   TF_BC_WALL : no-slip (sign = -1) or free-slip (sign = +1) wall,
+ *                BoundaryConditions.py:55-233;
+ *   TF_BC_FORCE: _constant_forcing_* with forcing constant fc and atom
+ *                constant ac for variable var, BoundaryConditions.py:471-544
+ *                (moving lids, fixed temperatures and heat fluxes reduce to
+ *                this).                                                       */
+typedef struct tf_bc_op {
+    int32_t kind;
+    int32_t axis;   /* 0 = x, 1 = y, 2 = z                */
+    int32_t high;   /* 1 = east/north/top, 0 = west/...   */
+    int32_t var;    /* WALL: sign (+1/-1); FORCE: variable */
+    double fc;
+    double ac;
+} tf_bc_op;
+
+/* Scalars of Discretization._linear_part_2D/3D (Discretization.py:229-317)
+ * and the boundary program, plus the per-axis metric table.
+ * metric: device pointer to double[3][TF_METRIC_FIELDS][metric_stride] with
+ * fields, for cell m of face coordinates c:
+ *   D = c[m]-c[m-1], Dp = c[m+1]-c[m], H = (c[m]-c[m-2])/2,
+ *   Hp = (c[m+1]-c[m-1])/2, rD = 1/D, rDp = 1/Dp, rH = 1/H, rHp = 1/Hp,
+ *   w0 = 1/2*D/Hp, w1 = 1/2*Dp/Hp.                                          */
+#define TF_METRIC_FIELDS 10
+
+typedef struct tf_problem {
+    int32_t nx, ny, nz, dim, dof;
+    int32_t nonlinear;     /* 0 when Re == 0 and there is no temperature     */
+    int32_t buoy_row;      /* velocity row with the buoyancy term, -1 none   */
+    int32_t biot_row;      /* velocity column of the Biot term, -1 none      */
+    double visc;           /* 1 / (Re * sqrt(Gr))                            */
+    double cond;           /* 1 / (Pr * sqrt(Gr))                            */
+    double biot;           /* Bi / (Bi + 1)                                  */
+    const double *d_metric;
+    int32_t metric_stride;
+    int32_t nops;
+    tf_bc_op ops[TF_MAX_BC_OPS];
+} tf_problem;
+
+/* ---- library ------------------------------------------------------------*/
+
+int tf_version(void);
+const char *tf_error_string(int code);
+/* Number of kernel launches (and device memsets) the library has issued
+ * since load or the last reset; host-side counter, no synchronisation.      */
+long long tf_launch_count(void);
+void tf_launch_count_reset(void);
+
+/* ---- stencil CSR ----------------------------------------------------------
+ * The Jacobian is stored as a CSR whose rows have a fixed width per
+ * variable: every cell stores, for each of its dof rows, the structural
+ * superset of the reference's entries (all (d2, offset) an atom can hold),
+ * sorted by column.  Entries whose neighbour cell lies outside the grid are
+ * kept as zeros with a clamped column.  Row r = cell*dof + d1 starts at
+ * cell*width + row_offset[d1].                                              */
+
+/* Host query: cell width and per-variable row offsets (dof + 1 ints) and the
+ * slot table slot[(d1*dof + d2)*27 + ox + 3*oy + 9*oz] (-1: not stored).    */
+int tf_stencil_layout(int dim, int dof, int *row_offset, int *slot);
+
+/* rowptr[n+1] and cols[nnz] of the stencil CSR for the grid of p.          */
+int tf_stencil_pattern(const tf_problem *p, int32_t *d_rowptr, int32_t *d_cols,
+                       tf_stream_t stream);
+
+/* Fused assembly: F(x) into d_rhs and/or the Jacobian values into d_jvals
+ * (either may be NULL).  Bit-compatible with the reference's floating-point
+ * operation order.  Values with |v| <= 1e-14 are stored as 0.                */
+int tf_assemble(const tf_problem *p, const double *d_state, double *d_rhs,
+                double *d_jvals, tf_stream_t stream);
+
+/* Diagonal of the mass matrix (pressure entries 0).                          */
+int tf_mass_diag(const tf_problem *p, double *d_diag, tf_stream_t stream);
+
+/* Export to the reference's compressed CSR: drop zeros, merge duplicate
+ * columns in stored order (CrsMatrix.compress).  Two passes: call with
+ * d_out_cols == NULL to get d_out_rowptr (n+1) and *nnz (host), then again
+ * with output arrays of that size.                                           */
+int tf_csr_compact(int n, const int32_t *d_rowptr, const int32_t *d_cols,
+                   const double *d_vals, int32_t *d_out_rowptr, int32_t *d_out_cols,
+                   double *d_out_vals, int64_t *nnz, void *d_work, size_t work_bytes,
+                   tf_stream_t stream);
+size_t tf_csr_compact_workspace_bytes(int n);
+
+/* Copy of d_vals with the pressure gauge applied (row and column g replaced
+ * by a single -1 on the diagonal), as the SciPy backend does before splu.   */
+int tf_gauge_values(int n, const int32_t *d_rowptr, const int32_t *d_cols,
+                    const double *d_vals, int gauge, double *d_out, tf_stream_t stream);
+
+/* y = alpha * A x + beta * y (beta == 0: y is not read).                     */
+int tf_spmv_f64(int n, const int32_t *d_rowptr, const int32_t *d_cols,
+                const double *d_vals, const double *d_x, double *d_y,
+                double alpha, double beta, tf_stream_t stream);
+int tf_spmv_f32(int n, const int32_t *d_rowptr, const int32_t *d_cols,
+                const float *d_vals, const double *d_x, double *d_y,
+                double alpha, double beta, tf_stream_t stream);
+
+/* y[i] += a * diag[i] * x[i] (diagonal matrix product used by theta-method
+ * residuals and J - M / (theta dt)).                                         */
+int tf_diag_axpy(int n, double a, const double *d_diag, const double *d_x, double *d_y,
+                 tf_stream_t stream);
+/* vals[diag slot of row r] += a * diag[r] for every row with a stored
+ * diagonal (rows of the stencil CSR always store one).                      */
+int tf_add_diagonal(int n, const int32_t *d_rowptr, const int32_t *d_cols, double *d_vals,
+                    double a, const double *d_diag, tf_stream_t stream);
+
+/* ---- dense vector kernels (GMRES, continuation) -------------------------*/
+
+/* out[j] = sum_i V[j*ldv + i] * w[i] for j < k  (k <= 256); deterministic
+ * two-pass reduction; out is device memory.                                  */
+int tf_vec_mdot(int n, int k, const double *d_V, long long ldv, const double *d_w,
+                double *d_out, void *d_work, size_t work_bytes, tf_stream_t stream);
+size_t tf_vec_mdot_workspace_bytes(int n, int k);
+/* w[i] -= sum_j V[j*ldv+i] * h[j]  (h device, k <= 256)                     */
+int tf_vec_mgs_update(int n, int k, const double *d_V, long long ldv, const double *d_h,
+                      double *d_w, tf_stream_t stream);
+/* z = a x + b y (x or y may be NULL, meaning absent; z may alias x or y).    */
+int tf_vec_axpby(int n, double a, const double *d_x, double b, const double *d_y,
+                 double *d_z, tf_stream_t stream);
+/* z = x / s, IEEE division per element (z may alias x).                      */
+int tf_vec_div(int n, const double *d_x, double s, double *d_z, tf_stream_t stream);
+int tf_vec_fill(int n, double a, double *d_z, tf_stream_t stream);
+int tf_vec_to_f32(int n, const double *d_x, float *d_y, tf_stream_t stream);
+
+/* ---- nested-dissection multifrontal LU (tf_nd.cu) ------------------------*/
+
+typedef struct tf_nd_plan {
+    int32_t n;            /* unknowns                                        */
+    int32_t nnodes;
+    int32_t nlevels;
+    const int32_t *level_ptr;   /* host: nodes of height h are              */
+                                /* [level_ptr[h], level_ptr[h+1])            */
+    const int32_t *max_own;     /* host: per level max own size              */
+    const int32_t *max_f;       /* host: per level max front size            */
+    const int32_t *d_n_own;
+    const int32_t *d_f;
+    const int32_t *d_parent;
+    const int64_t *d_front_off; /* nnodes + 1                                */
+    const int64_t *d_idx_off;   /* nnodes + 1                                */
+    const int32_t *d_idx;       /* own then boundary unknowns per node        */
+    const int64_t *d_ea_off;    /* nnodes + 1                                */
+    const int32_t *d_ea_map;    /* child boundary -> parent front position   */
+    int64_t nscat;
+    const int64_t *d_scat_pos;  /* front element receiving each entry         */
+    const int32_t *d_scat_src;  /* stencil-CSR entry index                    */
+    const int64_t *scat_level_ptr; /* host: entries of level h               */
+    const int64_t *d_piv_off;   /* nnodes + 1: pivot storage offsets (own)    */
+    const int32_t *d_rank;      /* 0/1: position among the parent's children  */
+    int64_t front_elems;        /* total front elements                       */
+} tf_nd_plan;
+
+/* Numeric factorisation of the (gauged) stencil-CSR values.  d_fronts holds
+ * plan->front_elems elements of the factor precision; d_piv holds plan->n
+ * int32.  d_info (device int32, may be NULL) is incremented once per exactly
+ * zero pivot (the pivot is then replaced by 1e-30 and the solve is useless).*/
+int tf_nd_factor_f64(const tf_nd_plan *plan, const double *d_vals, double *d_fronts,
+                     int32_t *d_piv, int32_t *d_info, tf_stream_t stream);
+int tf_nd_factor_f32(const tf_nd_plan *plan, const double *d_vals, float *d_fronts,
+                     int32_t *d_piv, int32_t *d_info, tf_stream_t stream);
+/* In-place solve of the factored system: d_x (length n, FP64) holds the
+ * right-hand side on entry and the solution on exit.  The f32 variant works
+ * in single precision on the FP64 vector.                                    */
+int tf_nd_solve_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_t *d_piv,
+                    double *d_x, tf_stream_t stream);
+int tf_nd_solve_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,
+                    double *d_x, tf_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TFCUDA_H */

@@ -1,0 +1,75 @@
+"""GPU linear solves against the reference SciPy backend (splu) fixtures and
+against SciPy on larger grids."""
+
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spla
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _gauged(A, g):
+    import scipy.sparse as sp
+    A = A.tocoo()
+    keep = (A.row != g) & (A.col != g)
+    return sp.csr_matrix((np.append(A.data[keep], -1.0), (np.append(A.row[keep], g), np.append(A.col[keep], g))),
+                         shape=A.shape)
+
+
+def test_direct_solve_matches_reference():
+    from transiflow_gb300 import Interface
+    g = load_golden('solve_ldc2d_12')
+    itf = Interface({'Reynolds Number': float(g['re'])}, 12, 12)
+    J = itf.jacobian(itf.vector_from_array(g['state']))
+    y = itf.solve(J, itf.vector_from_array(g['b'])).numpy()
+    assert np.linalg.norm(y - g['y']) / np.linalg.norm(g['y']) < 1e-10
+
+
+def test_bordered_solve_matches_reference():
+    from transiflow_gb300 import Interface
+    g = load_golden('solve_ldc2d_12')
+    itf = Interface({'Reynolds Number': float(g['re'])}, 12, 12)
+    J = itf.jacobian(itf.vector_from_array(g['state']))
+    y1, y2 = itf.solve(J, itf.vector_from_array(g['b']), float(g['rhs2']), itf.vector_from_array(g['V']),
+                       itf.vector_from_array(g['W']), float(g['C']))
+    assert np.linalg.norm(y1.numpy() - g['y1']) / np.linalg.norm(g['y1']) < 1e-9
+    assert abs(y2 - float(g['y2'])) <= 1e-9 * abs(float(g['y2']))
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32'])
+@pytest.mark.parametrize('shape,params', [((48, 48, 1), {'Reynolds Number': 2000}),
+                                          ((24, 20, 1), {'Problem Type': 'Differentially Heated Cavity',
+                                                         'Rayleigh Number': 1e5, 'Prandtl Number': 1000,
+                                                         'Reynolds Number': 1, 'Grid Stretching Factor': 1.5}),
+                                          ((8, 8, 6), {'Reynolds Number': 300})])
+def test_nd_gmres_solves_gauged_system(precision, shape, params):
+    from transiflow_gb300 import Interface
+    p = dict(params)
+    p['CUDA'] = {'Factor Precision': precision, 'Tolerance': 1e-12}
+    nx, ny, nz = shape
+    itf = Interface(p, nx, ny, nz)
+    rng = np.random.default_rng(3)
+    x = itf.vector_from_array(0.5 * rng.standard_normal(itf.n))
+    J = itf.jacobian(x)
+    b = rng.standard_normal(itf.n)
+    y = itf.solve(J, itf.vector_from_array(b)).numpy()
+    A = _gauged(J.to_scipy(), itf.dim)
+    bg = b.copy()
+    bg[itf.dim] = 0
+    assert np.linalg.norm(A @ y - bg) / np.linalg.norm(bg) < 1e-11
+    ref = spla.spsolve(A.tocsc(), bg)
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-8
+    # the factorisation is cached on the matrix: a second solve reuses it
+    nf = itf.solver.stats['factorizations']
+    itf.solve(J, itf.vector_from_array(b))
+    assert itf.solver.stats['factorizations'] == nf
+
+
+def test_zero_rhs_gives_zero():
+    from transiflow_gb300 import Interface
+    itf = Interface({'Reynolds Number': 10}, 8, 8)
+    J = itf.jacobian(itf.vector())
+    y = itf.solve(J, itf.vector())
+    assert np.all(y.numpy() == 0)

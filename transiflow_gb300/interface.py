@@ -1,0 +1,231 @@
+"""The ``CUDA`` backend behind TransiFlow's interface contract.
+
+``Interface`` has the constructor signature of
+``transiflow.interface.BaseInterface`` (BaseInterface.py:45-46) and
+provides the methods the drivers call -- ``vector``, ``rhs``, ``jacobian``,
+``mass_matrix``, ``solve`` (SciPy.py:37-49, 311-315), ``set_parameter`` /
+``get_parameter`` (BaseInterface.py:94-116), ``save_state`` /
+``load_state`` (BaseInterface.py:118-215) and ``vector_from_array`` /
+``array_from_vector`` -- so ``Continuation`` and ``TimeIntegration`` run on
+it unchanged.  States live on the GPU as :class:`DeviceVector`; the
+discretisation, the Jacobian and the solves run in libtfcuda kernels.
+``eigs`` is not provided (docs/custom-backend.rst allows that).
+
+Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
+  'Factor Precision'  'fp64' (default) or 'fp32' for the preconditioner LU
+  'Tolerance'         GMRES relative residual (default 1e-12)
+  'Restart'           GMRES restart length (default 50)
+  'Maximum Iterations'  GMRES iteration cap (default 500)
+  'Fuse Jacobian'     compute the Jacobian together with the RHS and reuse it
+                      when jacobian() is called at the same state and
+                      parameters (default False)
+"""
+
+import ctypes
+import json
+
+import numpy as np
+import torch
+
+from . import _lib, grid
+from .matrix import DiagonalMatrix, Pattern, StencilMatrix
+from .solver import Solver
+from .vector import DeviceVector, _stream
+
+
+class _NumpyEncoder(json.JSONEncoder):
+    def default(self, obj):
+        if isinstance(obj, np.integer):
+            return int(obj)
+        if isinstance(obj, np.floating):
+            return float(obj)
+        if isinstance(obj, (complex, np.complexfloating)):
+            return {'__complex__': True, 'real': obj.real, 'imag': obj.imag}
+        if isinstance(obj, np.ndarray):
+            return obj.tolist()
+        return json.JSONEncoder.default(self, obj)
+
+
+def _decode(obj):
+    if '__complex__' in obj:
+        return complex(obj['real'], obj['imag'])
+    return obj
+
+
+class Interface:
+    def __init__(self, parameters, nx, ny, nz=1, dim=None, dof=None, x=None, y=None, z=None,
+                 boundary_conditions=None, device=None):
+        if not torch.cuda.is_available():
+            raise _lib.CudaBackendError('the CUDA backend needs a GPU')
+        self.lib = _lib.load()
+        self.device = torch.device(device or 'cuda')
+        self.parameters = parameters
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.dim = dim if dim is not None else (3 if nz > 1 else 2)
+        self.dof = dof if dof is not None else grid.default_dof(parameters, self.dim)
+        self.boundary_conditions = boundary_conditions
+        p = parameters
+        self.x = np.asarray(x) if x is not None else grid.coordinate_vector(p, p.get('X-min', 0.0), p.get('X-max', 1.0), nx)
+        self.y = np.asarray(y) if y is not None else grid.coordinate_vector(p, p.get('Y-min', 0.0), p.get('Y-max', 1.0), ny)
+        self.z = np.asarray(z) if z is not None else grid.coordinate_vector(p, p.get('Z-min', 0.0), p.get('Z-max', 1.0), nz)
+        self.n = nx * ny * nz * self.dof
+        self.pressure_row = self.dim
+        self.border_scaling = 1e-3
+        table = grid.metric_table((self.x, self.y, self.z), (nx, ny, nz))
+        self._metric = torch.as_tensor(table.ravel()).to(self.device)
+        self._stride = table.shape[2]
+        # validate the problem type and boundary program now
+        self._problem()
+        # pattern of the stencil CSR
+        row_offset = np.zeros(self.dof + 1, dtype=np.int32)
+        slot = np.zeros(self.dof * self.dof * 27, dtype=np.int32)
+        _lib.check(self.lib.tf_stencil_layout(self.dim, self.dof, row_offset.ctypes.data, slot.ctypes.data),
+                   'tf_stencil_layout')
+        width = int(row_offset[-1])
+        ncell = nx * ny * nz
+        rowptr = torch.empty(self.n + 1, dtype=torch.int32, device=self.device)
+        cols = torch.empty(ncell * width, dtype=torch.int32, device=self.device)
+        prob = self._problem()
+        _lib.check(self.lib.tf_stencil_pattern(ctypes.byref(prob), rowptr.data_ptr(), cols.data_ptr(), _stream()),
+                   'tf_stencil_pattern')
+        self.pattern = Pattern(rowptr, cols, self.n, width, row_offset, slot.reshape(self.dof, self.dof, 27))
+        opts = parameters.get('CUDA', {})
+        self.solver = Solver(self, restart=opts.get('Restart', 50), tol=opts.get('Tolerance', 1e-12),
+                             maxit=opts.get('Maximum Iterations', 500),
+                             precision=opts.get('Factor Precision', 'fp64'))
+        self.fuse = opts.get('Fuse Jacobian', False)
+        self._cached_jac = None
+        self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}
+
+    # -- parameters (BaseInterface.py:94-116, Discretization.py:145-184) -------
+    def set_parameter(self, name, value):
+        if name in self.parameters and self.get_parameter(name) == value:
+            return
+        self.parameters[name] = value
+
+    def get_parameter(self, name, default=0):
+        return self.parameters.get(name, default) if name in self.parameters else default
+
+    def _problem(self):
+        return grid.make_problem(self.parameters, self.nx, self.ny, self.nz, self.dim, self.dof,
+                                 self.x, self.y, self.z, self._metric.data_ptr(), self._stride,
+                                 self.boundary_conditions)
+
+    # -- vectors -----------------------------------------------------------------
+    def vector(self):
+        return DeviceVector.zeros(self.n, self.device)
+
+    def vector_from_array(self, array):
+        return DeviceVector.from_array(np.asarray(array), self.device)
+
+    def array_from_vector(self, vector):
+        return vector.numpy() if isinstance(vector, DeviceVector) else np.asarray(vector)
+
+    def _as_device(self, state):
+        if isinstance(state, DeviceVector):
+            return state
+        return DeviceVector.from_array(np.asarray(state), self.device)
+
+    # -- discretisation ------------------------------------------------------
+    def _key(self, state):
+        return (state.data.data_ptr(), state.data._version, json.dumps(self.parameters, sort_keys=True,
+                                                                     cls=_NumpyEncoder, default=str))
+
+    def rhs(self, state):
+        """F(state), Discretization.rhs (Discretization.py:367-390)."""
+        self.calls['rhs'] += 1
+        x = self._as_device(state)
+        out = torch.empty(self.n, dtype=torch.float64, device=self.device)
+        prob = self._problem()
+        jv = None
+        if self.fuse:
+            jv = torch.empty(self.pattern.nnz, dtype=torch.float64, device=self.device)
+        _lib.check(self.lib.tf_assemble(ctypes.byref(prob), x.data.data_ptr(), out.data_ptr(),
+                                        None if jv is None else jv.data_ptr(), _stream()), 'tf_assemble')
+        if jv is not None:
+            self._cached_jac = (self._key(x), jv)
+        result = DeviceVector(out)
+        return result if isinstance(state, DeviceVector) else result.numpy()
+
+    def jacobian(self, state):
+        """J(state) in the stencil CSR, Discretization.jacobian (Discretization.py:392-415)."""
+        self.calls['jacobian'] += 1
+        x = self._as_device(state)
+        if self._cached_jac is not None and self._cached_jac[0] == self._key(x):
+            self.calls['fused_jacobians'] += 1
+            jv = self._cached_jac[1]
+            self._cached_jac = None
+            return StencilMatrix(self.pattern, jv)
+        jv = torch.empty(self.pattern.nnz, dtype=torch.float64, device=self.device)
+        prob = self._problem()
+        _lib.check(self.lib.tf_assemble(ctypes.byref(prob), x.data.data_ptr(), None, jv.data_ptr(), _stream()),
+                   'tf_assemble')
+        return StencilMatrix(self.pattern, jv)
+
+    def mass_matrix(self):
+        """Diagonal mass matrix, Discretization.mass_matrix (Discretization.py:417-548)."""
+        d = torch.empty(self.n, dtype=torch.float64, device=self.device)
+        prob = self._problem()
+        _lib.check(self.lib.tf_mass_diag(ctypes.byref(prob), d.data_ptr(), _stream()), 'tf_mass_diag')
+        return DiagonalMatrix(d)
+
+    # -- solves -----------------------------------------------------------------
+    def solve(self, jac, rhs, rhs2=None, V=None, W=None, C=None):
+        """Solve J y = rhs (or the bordered system), SciPy.Interface.solve (SciPy.py:311-315)."""
+        self.calls['solve'] += 1
+        host = not isinstance(rhs, DeviceVector)
+        out = self.solver.solve(jac, rhs, rhs2, V, W, C)
+        if rhs2 is None:
+            return out.numpy() if host else out
+        y, y2 = out
+        return (y.numpy() if host else y), y2
+
+    def eigs(self, state, return_eigenvectors=False, enable_recycling=False):
+        raise NotImplementedError('the CUDA backend has no eigenvalue solver')
+
+    # -- checkpointing (BaseInterface.py:118-215) ---------------------------------
+    def save_json(self, name, obj):
+        with open(name, 'w') as f:
+            json.dump(obj, f, cls=_NumpyEncoder)
+
+    def save_parameters(self, name):
+        self.save_json(name + '.params', self.parameters)
+        print('Wrote parameters to', name + '.params', flush=True)
+
+    def save_state(self, name, x):
+        self.save_parameters(name)
+        if not name.endswith('.npy'):
+            name += '.npy'
+        np.save(name, self.array_from_vector(x))
+        print('Wrote state to', name, flush=True)
+
+    def load_json(self, name):
+        with open(name, 'r') as f:
+            return json.load(f, object_hook=_decode)
+
+    def load_parameters(self, name):
+        old = self.parameters.copy()
+        self.parameters.update(self.load_json(name + '.params'))
+        print('Read parameters from', name + '.params', flush=True)
+        for k, v in self.parameters.items():
+            if v != old.get(k):
+                print("Updated '{}' from {} to {}".format(k, old.get(k), v), flush=True)
+
+    def load_state(self, name):
+        self.load_parameters(name)
+        if not name.endswith('.npy'):
+            name += '.npy'
+        x = np.load(name)
+        print('Read state from', name, flush=True)
+        return self.vector_from_array(x)
+
+
+def create(parameters, nx, ny, nz=1, dim=None, dof=None, boundary_conditions=None, backend='CUDA'):
+    """transiflow.interface.create with a 'CUDA' backend (create.py:4-68).
+
+    Other backend names are delegated to the reference package when it is
+    importable."""
+    if backend.lower() == 'cuda':
+        return Interface(parameters, nx, ny, nz, dim, dof, boundary_conditions=boundary_conditions)
+    from transiflow.interface import create as ref_create   # the reference's own backends
+    return ref_create(parameters, nx, ny, nz, dim, dof, boundary_conditions=boundary_conditions, backend=backend)
