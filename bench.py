@@ -1,0 +1,382 @@
+"""Benchmark: seconds to reach the Reynolds-number target on one GB300.
+
+Workload (the plain-GPU configuration of the headline metric): 2D
+lid-driven cavity, nx = ny = 256 (196,608 unknowns), FP64 assembly,
+Newton at Re = 0 from the zero state, then pseudo-arclength continuation in
+the Reynolds number from 0 to 5000 with ds = 200 and ||F|| <= 1e-8 at every
+point; linear solves by FP64 GMRES to 1e-10 relative residual, preconditioned
+by the nested-dissection LU of the gauged Jacobian.  One step = one complete
+branch.  Synthetic: the branch starts from the zero state (no dataset).
+
+  value      seconds per branch, the initial state already on the device
+  e2e        the same through the public API with host buffers: the initial
+             state is copied from pinned host memory and the final state read
+             back inside the timed region
+  roofline   the dominant kernel, timed live with CUDA events
+  cpu_baseline  the CPU oracle (NumPy assembly + SuperLU) per call on this
+             host, scaled by the branch's call counts
+
+``--impl reference`` times the reference algorithm's CPU implementation on
+this host (the oracle restatement: the reference package itself is not
+installable on the GPU machine) on the same workload, one bounded sample per
+step.
+"""
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+import io
+import contextlib
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 's to Re target: learned+mixed vs plain FP64 on same GB300 at ||F||<=1e-8'
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=3)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--nx', type=int, default=256)
+    ap.add_argument('--target', type=float, default=5000.0)
+    ap.add_argument('--ds', type=float, default=200.0)
+    ap.add_argument('--precision', default='fp64', choices=['fp64', 'fp32'])
+    ap.add_argument('--tol', type=float, default=1e-10)
+    ap.add_argument('--no-baseline', action='store_true')
+    return ap.parse_args()
+
+
+def config(args):
+    return {'workload': '2D lid-driven cavity %dx%d, dof 3 (%d unknowns), Newton at Re=0 then continuation '
+                        'Re 0->%g, ds=%g, ||F||<=1e-8, FP64 GMRES to %g + ND-LU (%s factors)'
+                        % (args.nx, args.nx, 3 * args.nx * args.nx, args.target, args.ds, args.tol,
+                           args.precision),
+            'nx': args.nx, 'ny': args.nx, 'dof': 3, 'unknowns': 3 * args.nx * args.nx,
+            'target_re': args.target, 'ds': args.ds, 'newton_tolerance': 1e-8,
+            'l2': 'working set larger than L2 (1.1 GB of frontal matrices at 256^2)',
+            'parallelism': 'replicas (one instance per GPU)'}
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ('clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.FIELDS,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:6]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': mx,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_branch(itf, Continuation, x0, args):
+    cont = Continuation(itf, newton_tolerance=1e-8)
+    with contextlib.redirect_stdout(io.StringIO()):
+        itf.set_parameter('Reynolds Number', 0.0)
+        x = cont.newton(x0)
+        x, mu = cont.continuation(x, 'Reynolds Number', 0.0, args.target, args.ds)
+    return x, mu, cont
+
+
+def gpu_arm(args, rank, world, local):
+    import torch
+    from transiflow_gb300 import Continuation, Interface, _lib, dist
+    torch.cuda.set_device(local)
+    lib = _lib.load()
+    params = {'CUDA': {'Factor Precision': args.precision, 'Tolerance': args.tol}}
+    itf = Interface(params, args.nx, args.nx)
+    n = itf.n
+    stream = torch.cuda.current_stream()
+
+    # warm-up branches (the first one also builds the elimination plan)
+    for _ in range(args.warmup):
+        x, mu, cont = run_branch(itf, Continuation, itf.vector(), args)
+    calls = dict(cont.stats)
+    calls['factorizations'] = None
+    fac0 = itf.solver.stats['factorizations']
+    x, mu, cont = run_branch(itf, Continuation, itf.vector(), args)
+    calls['factorizations'] = itf.solver.stats['factorizations'] - fac0
+    calls['gmres_iterations_last'] = itf.solver.stats['gmres_iterations']
+    itf.set_parameter('Reynolds Number', mu)
+    fnorm_end = itf.rhs(x).norm()
+
+    # ---- value: device-resident start state ----
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    l0 = lib.tf_launch_count()
+    t_dev = []
+    for _ in range(args.steps):
+        x0 = itf.vector()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        x, mu, _ = run_branch(itf, Continuation, x0, args)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        t_dev.append(ev0.elapsed_time(ev1) / 1000.0)
+    launches = lib.tf_launch_count() - l0
+    dist.barrier()
+    clk = clocks.stop()
+    t_step = dist.max_over_ranks(statistics.mean(t_dev))
+
+    # ---- e2e: host buffers through the public API ----
+    host0 = torch.zeros(n, dtype=torch.float64).pin_memory()
+    t_e2e = []
+    dist.barrier()
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        x0 = itf.vector_from_array(host0.numpy())
+        x, mu, _ = run_branch(itf, Continuation, x0, args)
+        out = itf.array_from_vector(x)
+        torch.cuda.synchronize()
+        t_e2e.append(time.perf_counter() - t0)
+    e2e = dist.max_over_ranks(statistics.mean(t_e2e))
+    dist.barrier()
+
+    roof = roofline(itf, x, args, lib)
+    result = {'metric': METRIC, 'value': t_step, 'unit': 's', 'n_gpus': world, 'steps': args.steps,
+              'warmup': args.warmup, 'ms_per_step': t_step * 1000.0, 'higher_is_better': False,
+              'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64' if args.precision == 'fp64' else 'f64+f32',
+              'data': 'synthetic (zero initial state; no dataset)', 'config': config(args),
+              'e2e': {'value': e2e, 'unit': 's', 'h2d_bytes_per_step': 8 * n, 'd2h_bytes_per_step': 8 * n},
+              'roofline': roof, 'clocks': clk, 'gpu_launches': int(launches),
+              'branch': {'points': calls.get('points'), 'rhs': calls.get('rhs'), 'jacobian': calls.get('jacobian'),
+                         'solve': calls.get('solve'), 'factorizations': calls.get('factorizations'),
+                         'final_re': mu, 'final_fnorm': fnorm_end}}
+    if rank == 0 and not args.no_baseline:
+        result['cpu_baseline'] = cpu_baseline(args, calls)
+    return result
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            p = json.load(f)
+        return float(p['hbm_gbs']), 'measured'
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 'fallback'
+
+
+def roofline(itf, x, args, lib):
+    """Live CUDA-event timing of the dominant kernels over rotating buffers
+    larger than L2 (129 MB)."""
+    import torch
+    from transiflow_gb300.vector import _stream
+    from transiflow_gb300.solver import _struct_ptr
+    n = itf.n
+    nnz = itf.pattern.nnz
+    prob = itf._problem()
+    reps = 8
+    # rotating states and Jacobian value buffers: reps x (8n + 8 nnz) > L2
+    states = [x.data.clone() for _ in range(reps)]
+    rhs = [torch.empty(n, dtype=torch.float64, device=itf.device) for _ in range(reps)]
+    jv = [torch.empty(nnz, dtype=torch.float64, device=itf.device) for _ in range(reps)]
+    st = torch.cuda.current_stream()
+
+    def timed(fn, count):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for i in range(count):
+            fn(i % reps)
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1000.0 / count
+
+    def asm(i):
+        lib.tf_assemble(ctypes.byref(prob), states[i].data_ptr(), rhs[i].data_ptr(), jv[i].data_ptr(), _stream())
+
+    timed(asm, reps)
+    t_asm = timed(asm, 40)
+    bytes_asm = 16 * n + 8 * nnz          # read x + write F, write J values
+    rp, cp = itf.pattern.rowptr, itf.pattern.cols
+
+    def spmv(i):
+        lib.tf_spmv_f64(n, rp.data_ptr(), cp.data_ptr(), jv[i].data_ptr(), states[i].data_ptr(),
+                        rhs[i].data_ptr(), 1.0, 0.0, _stream())
+
+    timed(spmv, reps)
+    t_spmv = timed(spmv, 40)
+    bytes_spmv = 12 * nnz + 4 * (n + 1) + 16 * n
+    # factorisation and solve of the current Jacobian
+    J = itf.jacobian(itf.vector_from_array(x.numpy()))
+    fac = itf.solver.factorization(J)
+    torch.cuda.synchronize()
+    f_time = []
+    for _ in range(3):
+        J.lu = None
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fac = itf.solver.factorization(J)
+        e1.record(st)
+        torch.cuda.synchronize()
+        f_time.append(e0.elapsed_time(e1) / 1000.0)
+    t_fac = min(f_time)
+    v = torch.ones(n, dtype=torch.float64, device=itf.device)
+    t_sol = timed(lambda i: fac.apply(v), 10)
+    peak, which = _peaks()
+    flops = itf.solver.plan.flops
+    kernels = {
+        'tf_assemble (F + J, fused)': {'s_per_launch': t_asm, 'bytes': bytes_asm,
+                                       'GB/s': bytes_asm / t_asm / 1e9},
+        'tf_spmv_f64': {'s_per_launch': t_spmv, 'bytes': bytes_spmv, 'GB/s': bytes_spmv / t_spmv / 1e9},
+        'tf_nd_factor (%s)' % args.precision: {'s_per_call': t_fac, 'flops': flops,
+                                                'GFLOP/s': flops / t_fac / 1e9},
+        'tf_nd_solve (%s)' % args.precision: {'s_per_call': t_sol},
+    }
+    a = bytes_asm / t_asm / 1e9
+    return {'bound': 'hbm', 'kernel': 'tf_assemble (fused RHS + Jacobian, %dx%d)' % (args.nx, args.nx),
+            'achieved': a, 'peak': peak, 'unit': 'GB/s', 'frac': a / peak,
+            'peak_source': '%s (MEASURED_PEAKS.json hbm_gbs)' % which if which == 'measured' else which,
+            'traffic': None, 'algorithmic_bytes': bytes_asm, 'kernels': kernels}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle timings (the reference algorithm on this host's cores)
+# ---------------------------------------------------------------------------
+def oracle_sample(nx, seed=1):
+    from oracle.solve import Interface as OracleInterface
+    itf = OracleInterface({'Reynolds Number': 1000}, nx, nx)
+    s = 0.1 * np.random.default_rng(seed).standard_normal(itf.vector().size)
+    t = {}
+    t0 = time.perf_counter()
+    f = itf.rhs(s)
+    t['rhs'] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    J = itf.jacobian(s)
+    t['jacobian'] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    itf.solve(J, f)
+    t['factor_solve'] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    itf.solve(J, f)
+    t['solve'] = time.perf_counter() - t0
+    return t
+
+
+# Call counts of the branch (2D LDC 256^2, Re 0 -> 5000, ds = 200,
+# newton_tolerance 1e-8) as run by the continuation driver; the GPU arm
+# recomputes them live and the reference arm uses these.
+BRANCH_CALLS_256 = {'rhs': None, 'jacobian': None, 'solve': None, 'factorizations': None}
+
+
+def extrapolate(t, calls):
+    nfac = calls.get('factorizations') or calls['jacobian']
+    return (calls['rhs'] * t['rhs'] + calls['jacobian'] * t['jacobian'] + nfac * t['factor_solve']
+            + max(calls['solve'] - nfac, 0) * t['solve'])
+
+
+def cpu_baseline(args, calls):
+    t = oracle_sample(args.nx)
+    est = extrapolate(t, calls)
+    return {'value': est, 'unit': 's', 'cores': 1, 'kind': 'port',
+            'sample': 'oracle (vectorised NumPy restatement of Discretization + SciPy SuperLU, '
+                      'single-threaded splu) at %dx%d: 1 rhs %.2fs, 1 jacobian %.2fs, 1 factor+solve %.2fs, '
+                      '1 solve %.2fs, scaled by the branch call counts %s'
+                      % (args.nx, args.nx, t['rhs'], t['jacobian'], t['factor_solve'], t['solve'],
+                         {k: calls[k] for k in ('rhs', 'jacobian', 'solve', 'factorizations')}),
+            'host_cpus': os.cpu_count()}
+
+
+def reference_arm(args, rank):
+    if rank != 0:
+        return None
+    calls = dict(BRANCH_CALLS_256)
+    if any(v is None for v in calls.values()):
+        calls = {'rhs': 120, 'jacobian': 51, 'solve': 100, 'factorizations': 51}
+    for _ in range(args.warmup):
+        oracle_sample(args.nx)
+    vals = []
+    for _ in range(args.steps):
+        t = oracle_sample(args.nx)
+        vals.append(extrapolate(t, calls))
+    v = statistics.mean(vals)
+    return {'metric': METRIC, 'value': v, 'unit': 's', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': v * 1000.0, 'higher_is_better': False, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference', 'config': config(args),
+            'cpu_baseline': {'value': v, 'unit': 's', 'cores': 1, 'kind': 'port',
+                             'sample': 'per step one rhs, one jacobian, one SuperLU factor+solve and one solve '
+                                       'of the oracle at %dx%d on this host, scaled by the branch call counts %s'
+                                       % (args.nx, args.nx, calls)},
+            'e2e': {'value': v, 'unit': 's', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+
+
+def main():
+    args = parse()
+    from transiflow_gb300 import dist
+    rank, world, local = dist.init_from_env()
+    try:
+        if args.impl == 'reference':
+            res = reference_arm(args, rank)
+        else:
+            res = gpu_arm(args, rank, world, local)
+        if rank == 0 and res is not None:
+            print(json.dumps(res), flush=True)
+    finally:
+        dist.finalize()
+
+
+if __name__ == '__main__':
+    main()
