@@ -170,6 +170,18 @@ int tf_add_diagonal(int n, const int32_t *d_rowptr, const int32_t *d_cols, doubl
 int tf_vec_mdot(int n, int k, const double *d_V, long long ldv, const double *d_w,
                 double *d_out, void *d_work, size_t work_bytes, tf_stream_t stream);
 size_t tf_vec_mdot_workspace_bytes(int n, int k);
+/* Same result as tf_vec_mdot, for callers that cannot allocate device
+ * memory (no counterpart in the reference): a host application that gives
+ * the library a fixed device-memory budget and forbids further cudaMalloc,
+ * or a loop that must not incur the device-wide synchronisation of
+ * cudaMalloc/cudaFree.  The partial sums live in a fixed 152 KiB device array
+ * inside the library that every GPU loading it holds until exit; nothing is
+ * allocated per call.  k must not exceed 64 (TF_ERR_SIZE otherwise).  The
+ * first call on a device looks up the array's device address with that
+ * device current; make that first call before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race.                */
+int tf_vec_mdot_noalloc(int n, int k, const double *d_V, long long ldv, const double *d_w,
+                        double *d_out, tf_stream_t stream);
 /* w[i] -= sum_j V[j*ldv+i] * h[j]  (h device, k <= 256)                     */
 int tf_vec_mgs_update(int n, int k, const double *d_V, long long ldv, const double *d_h,
                       double *d_w, tf_stream_t stream);

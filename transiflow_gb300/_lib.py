@@ -109,6 +109,7 @@ _SIGNATURES = {
     'tf_add_diagonal': ([_I, _P, _P, _P, _D, _P, _P], _I),
     'tf_vec_mdot': ([_I, _I, _P, ctypes.c_longlong, _P, _P, _P, ctypes.c_size_t, _P], _I),
     'tf_vec_mdot_workspace_bytes': ([_I, _I], ctypes.c_size_t),
+    'tf_vec_mdot_noalloc': ([_I, _I, _P, ctypes.c_longlong, _P, _P, _P], _I),
     'tf_vec_mgs_update': ([_I, _I, _P, ctypes.c_longlong, _P, _P, _P], _I),
     'tf_vec_axpby': ([_I, _D, _P, _D, _P, _P, _P], _I),
     'tf_vec_div': ([_I, _P, _D, _P, _P], _I),

@@ -2,6 +2,8 @@
 // gauge, export to the reference's compressed CSR, diagonal updates and the
 // deterministic reductions used by GMRES and the continuation driver.
 
+#include <mutex>
+
 #include "tf_common.cuh"
 
 namespace tf {
@@ -354,6 +356,66 @@ extern "C" int tf_vec_mgs_update(int n, int k, const double *d_V, long long ldv,
                                  tf_stream_t stream) {
     if (n <= 0 || k <= 0 || k > 256 || !d_V || !d_h || !d_w || ldv < n) return TF_ERR_ARG;
     mgs_update_kernel<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, k, d_V, ldv, d_h, d_w); launched();
+    return cuda_status();
+}
+
+// ---------------------------------------------------------------------------
+// Multi-dot without caller-provided or allocated scratch.
+//
+// Some callers cannot allocate device memory at the point where they need an
+// inner product: a host application that hands this library a fixed device
+// memory budget up front and forbids any further cudaMalloc, or a solver loop
+// that must not pay the implicit device-wide synchronisation cudaMalloc and
+// cudaFree can cause.  tf_vec_mdot_noalloc gives them the same reduction as
+// tf_vec_mdot with its per-block partial sums kept in a fixed array that every
+// GPU loading this library holds until the process exits.
+//
+// Limit: k <= TF_MDOT_NOALLOC_MAX_K vectors (the array holds RED_BLOCKS x
+// TF_MDOT_NOALLOC_MAX_K doubles, 152 KiB).  All calls share the array, so
+// calls that overlap on the GPU (different streams without ordering between
+// them) race and must not be issued.  Each call writes every partial sum it
+// later reads, so nothing has to be cleared between calls.
+// ---------------------------------------------------------------------------
+#define TF_MDOT_NOALLOC_MAX_K 64
+
+static __device__ __align__(256) double g_mdot_noalloc_scratch[RED_BLOCKS * TF_MDOT_NOALLOC_MAX_K];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[kMaxDevices] = {};
+}  // namespace
+
+// Device address of the scratch array for the current device.  The host
+// symbol g_mdot_noalloc_scratch is only a stand-in for the array, not a
+// device address, so the address is looked up once per device with that
+// device current and cached.
+static int noalloc_scratch(double **out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return TF_ERR_CUDA;
+    if (dev < 0 || dev >= kMaxDevices) return TF_ERR_SIZE;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_mdot_noalloc_scratch) != cudaSuccess || !p) return TF_ERR_CUDA;
+        g_noalloc_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return TF_OK;
+}
+
+extern "C" int tf_vec_mdot_noalloc(int n, int k, const double *d_V, long long ldv, const double *d_w,
+                                   double *d_out, tf_stream_t stream) {
+    if (n <= 0 || k <= 0 || !d_V || !d_w || !d_out || ldv < n) return TF_ERR_ARG;
+    if (k > TF_MDOT_NOALLOC_MAX_K) return TF_ERR_SIZE;
+    double *scratch = nullptr;
+    int e = noalloc_scratch(&scratch);
+    if (e) return e;
+    cudaStream_t s = (cudaStream_t)stream;
+    int nb = blocks_for(n, RED_THREADS);
+    if (nb > RED_BLOCKS) nb = RED_BLOCKS;
+    mdot_partial_kernel<<<nb, RED_THREADS, 0, s>>>(n, k, d_V, ldv, d_w, scratch); launched();
+    mdot_final_kernel<<<k, 128, 0, s>>>(nb, k, scratch, d_out); launched();
     return cuda_status();
 }
 
