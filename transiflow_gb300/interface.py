@@ -16,6 +16,14 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
   'Tolerance'         GMRES relative residual (default 1e-12)
   'Restart'           GMRES restart length (default 50)
   'Maximum Iterations'  GMRES iteration cap (default 500)
+  'Reuse Factorization'  precondition a new Jacobian with the latest
+                      factorisation and refactor only if GMRES needs more than
+                      'Reuse Iterations' (default 20) iterations (default True)
+  'Reuse Policy'      'cost' (default): reuse only while the extra GMRES
+                      iterations cost less than a factorisation (measured),
+                      backing off after failed attempts; 'always'
+  'CUDA Graphs'       replay the factorisation and solve launch sequences from
+                      captured CUDA graphs (default True)
   'Fuse Jacobian'     compute the Jacobian together with the RHS and reuse it
                       when jacobian() is called at the same state and
                       parameters (default False)
@@ -92,7 +100,11 @@ class Interface:
         opts = parameters.get('CUDA', {})
         self.solver = Solver(self, restart=opts.get('Restart', 50), tol=opts.get('Tolerance', 1e-12),
                              maxit=opts.get('Maximum Iterations', 500),
-                             precision=opts.get('Factor Precision', 'fp64'))
+                             precision=opts.get('Factor Precision', 'fp64'),
+                             reuse=opts.get('Reuse Factorization', True),
+                             reuse_maxit=opts.get('Reuse Iterations', 20),
+                             graphs=opts.get('CUDA Graphs', True),
+                             reuse_policy=opts.get('Reuse Policy', 'cost'))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

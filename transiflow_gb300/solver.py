@@ -25,6 +25,11 @@ from .ndplan import build_plan
 from .vector import DeviceVector, _stream
 
 
+# Elimination plans depend only on the grid shape and the variables, so
+# interfaces of the same shape share one (keyed by shape and device).
+_PLANS = {}
+
+
 class NdPlanDevice:
     """The elimination plan of one grid, uploaded once."""
 
@@ -94,42 +99,121 @@ class NdPlanDevice:
         self.flops = p.flops
 
 
-class Factorization:
-    """Gauged values and their multifrontal LU, owned by one StencilMatrix."""
+class GaugedOperator:
+    """The gauged copy of one Jacobian's values: the operator GMRES solves with."""
 
-    def __init__(self, solver, jac, precision):
-        self.solver = solver
-        self.precision = precision
+    def __init__(self, solver, jac):
         self.n = jac.pattern.n
+        self.jac = jac
         lib = _lib.load()
         pat = jac.pattern
-        self.gauged = torch.empty_like(jac.values)
+        self.values = torch.empty_like(jac.values)
         _lib.check(lib.tf_gauge_values(self.n, pat.rowptr.data_ptr(), pat.cols.data_ptr(), jac.values.data_ptr(),
-                                       solver.gauge, self.gauged.data_ptr(), _stream()), 'tf_gauge_values')
+                                       solver.gauge, self.values.data_ptr(), _stream()), 'tf_gauge_values')
+
+    def matvec(self, x, out):
+        lib = _lib.load()
+        pat = self.jac.pattern
+        _lib.check(lib.tf_spmv_f64(self.n, pat.rowptr.data_ptr(), pat.cols.data_ptr(), self.values.data_ptr(),
+                                   x.data_ptr(), out.data_ptr(), 1.0, 0.0, _stream()), 'tf_spmv_f64')
+
+
+class _Graphed:
+    """A libtfcuda launch sequence captured once in a CUDA graph and replayed.
+
+    The sequence reads and writes fixed buffers only, so every replay redoes
+    the same work on the buffers' current contents.  The first call runs the
+    sequence eagerly (it also initialises per-kernel attributes outside any
+    capture), the second captures it, later calls replay it."""
+
+    def __init__(self, fn, counter):
+        self.fn = fn
+        self.graph = None
+        self.calls = 0
+        self.kernels = 0
+        self.counter = counter
+        self.failed = False
+
+    def __call__(self):
+        self.calls += 1
+        if self.graph is not None:
+            self.graph.replay()
+            self.counter['graph_kernel_launches'] += self.kernels
+            return
+        if self.calls == 1 or self.failed:
+            self.fn()
+            return
+        lib = _lib.load()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        before = lib.tf_launch_count()
+        try:
+            with torch.cuda.graph(g, capture_error_mode='thread_local'):
+                self.fn()
+        except RuntimeError:
+            self.failed = True
+            self.fn()
+            return
+        self.kernels = lib.tf_launch_count() - before
+        self.graph = g
+        g.replay()
+        self.counter['graph_kernel_launches'] += self.kernels
+
+
+class Factorization:
+    """Multifrontal LU of a gauged operator in the solver's front buffers.
+
+    Only the most recent factorisation of a precision is valid: the fronts are
+    one buffer per solver.  It is applied as a preconditioner."""
+
+    def __init__(self, solver, op, precision):
+        self.solver = solver
+        self.precision = precision
+        self.op = op
         self.fronts, self.piv = solver._front_buffers(precision, self)
-        info = solver.info
-        info.zero_()
-        fn = lib.tf_nd_factor_f64 if precision == 'fp64' else lib.tf_nd_factor_f32
-        _lib.check(fn(_struct_ptr(solver.plan.struct), self.gauged.data_ptr(), self.fronts.data_ptr(),
-                      self.piv.data_ptr(), info.data_ptr(), _stream()), 'tf_nd_factor')
-        self.zero_pivots = None
-        self.jac = jac
+        eng = solver._engine(precision)
+        solver._copy(op.values, eng.staging)
+        eng.factor()
 
     def valid(self):
         return self.solver._owner.get(self.precision) is self
 
     def apply(self, x):
         """In place: x <- M^-1 x."""
-        lib = _lib.load()
-        fn = lib.tf_nd_solve_f64 if self.precision == 'fp64' else lib.tf_nd_solve_f32
-        _lib.check(fn(_struct_ptr(self.solver.plan.struct), self.fronts.data_ptr(), self.piv.data_ptr(),
-                      x.data_ptr(), _stream()), 'tf_nd_solve')
+        eng = self.solver._engine(self.precision)
+        self.solver._copy(x, eng.vec)
+        eng.solve()
+        self.solver._copy(eng.vec, x)
 
-    def matvec(self, x, out):
+
+class _Engine:
+    """Fixed buffers of one factor precision and the (graphed) launch
+    sequences that factor and apply the LU."""
+
+    def __init__(self, solver, precision, graphs):
         lib = _lib.load()
-        pat = self.jac.pattern
-        _lib.check(lib.tf_spmv_f64(self.n, pat.rowptr.data_ptr(), pat.cols.data_ptr(), self.gauged.data_ptr(),
-                                   x.data_ptr(), out.data_ptr(), 1.0, 0.0, _stream()), 'tf_spmv_f64')
+        plan = solver.plan
+        self.staging = torch.empty(solver.itf.pattern.nnz, dtype=torch.float64, device=solver.itf.device)
+        self.vec = torch.empty(plan.host.n, dtype=torch.float64, device=solver.itf.device)
+        fronts, piv = solver._fronts_raw(precision)
+        info = solver.info
+        fac_fn = lib.tf_nd_factor_f64 if precision == 'fp64' else lib.tf_nd_factor_f32
+        sol_fn = lib.tf_nd_solve_f64 if precision == 'fp64' else lib.tf_nd_solve_f32
+        sp = _struct_ptr(plan.struct)
+
+        def factor():
+            _lib.check(fac_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(), info.data_ptr(),
+                              _stream()), 'tf_nd_factor')
+
+        def solve():
+            _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(), _stream()),
+                       'tf_nd_solve')
+
+        if graphs:
+            self.factor = _Graphed(factor, solver.stats)
+            self.solve = _Graphed(solve, solver.stats)
+        else:
+            self.factor, self.solve = factor, solve
 
 
 def _struct_ptr(s):
@@ -140,8 +224,21 @@ def _struct_ptr(s):
 class Solver:
     """Per-interface solver state: the plan, factor buffers, Krylov workspace."""
 
-    def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64'):
+    def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
+                 reuse_maxit=20, graphs=True, reuse_policy='cost'):
         self.itf = interface
+        self.graphs = graphs
+        self._engines = {}
+        self.reuse = reuse
+        self.reuse_maxit = reuse_maxit
+        self._prec = None
+        # running cost estimates (seconds): one factorisation, one GMRES iteration
+        self._cost_factor = None
+        self._cost_iter = None
+        self._pending = []
+        self.reuse_policy = reuse_policy
+        self._fail_streak = 0
+        self._skip = 0
         self.gauge = interface.pressure_row if interface.dof > interface.dim else -1
         self.restart = restart
         self.tol = tol
@@ -154,16 +251,22 @@ class Solver:
         self._V = None
         self._Z = None
         self._mdot_work = None
-        self.stats = {'factorizations': 0, 'solves': 0, 'gmres_iterations': 0, 'last_relres': None}
+        self.stats = {'factorizations': 0, 'solves': 0, 'gmres_iterations': 0, 'last_relres': None,
+                      'reused': 0, 'refactored_after_reuse': 0, 'graph_kernel_launches': 0}
 
     def _ensure_plan(self, pattern):
         if self.plan is None:
             itf = self.itf
-            self.plan = NdPlanDevice(pattern, itf.nx, itf.ny, itf.nz, itf.dof,
-                                     itf.dim if itf.dof > itf.dim else None)
+            pvar = itf.dim if itf.dof > itf.dim else None
+            key = (itf.nx, itf.ny, itf.nz, itf.dim, itf.dof, pvar, str(pattern.rowptr.device))
+            plan = _PLANS.get(key)
+            if plan is None:
+                plan = NdPlanDevice(pattern, itf.nx, itf.ny, itf.nz, itf.dof, pvar)
+                _PLANS[key] = plan
+            self.plan = plan
             self.info = torch.zeros(1, dtype=torch.int32, device=pattern.rowptr.device)
 
-    def _front_buffers(self, precision, owner):
+    def _fronts_raw(self, precision):
         dt = torch.float64 if precision == 'fp64' else torch.float32
         bufs = self._fronts.get(precision)
         if bufs is None:
@@ -171,16 +274,46 @@ class Solver:
             bufs = (torch.empty(self.plan.front_elems, dtype=dt, device=dev),
                     torch.empty(self.plan.host.n, dtype=torch.int32, device=dev))
             self._fronts[precision] = bufs
+        return bufs
+
+    def _front_buffers(self, precision, owner):
+        bufs = self._fronts_raw(precision)
         self._owner[precision] = owner
         return bufs
 
-    def factorization(self, jac):
+    def _engine(self, precision):
+        eng = self._engines.get(precision)
+        if eng is None:
+            eng = _Engine(self, precision, self.graphs)
+            self._engines[precision] = eng
+        return eng
+
+    def operator(self, jac):
         self._ensure_plan(jac.pattern)
+        op = getattr(jac, '_gauged', None)
+        if op is None:
+            op = GaugedOperator(self, jac)
+            jac._gauged = op
+        return op
+
+    def factorize(self, op):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fac = Factorization(self, op, self.precision)
+        e1.record()
+        self._pending.append((e0, e1))
+        self.stats['factorizations'] += 1
+        self._prec = fac
+        op.jac.lu = fac
+        return fac
+
+    def factorization(self, jac):
+        """The factorisation of jac itself (computed if needed)."""
+        op = self.operator(jac)
         fac = jac.lu
-        if fac is None or not isinstance(fac, Factorization) or not fac.valid() or fac.precision != self.precision:
-            fac = Factorization(self, jac, self.precision)
-            jac.lu = fac
-            self.stats['factorizations'] += 1
+        if not isinstance(fac, Factorization) or not fac.valid() or fac.precision != self.precision:
+            fac = self.factorize(op)
         return fac
 
     # -- Krylov ---------------------------------------------------------------
@@ -192,7 +325,15 @@ class Solver:
             lib = _lib.load()
             wb = lib.tf_vec_mdot_workspace_bytes(n, m + 1)
             self._mdot_work = torch.empty((wb + 7) // 8 + m + 2, dtype=torch.float64, device=dev)
+            self._hbuf = torch.empty(2 * (m + 1), dtype=torch.float64, device=dev)
         return self._V, self._Z
+
+    def _mdot_into(self, V, k, w, out):
+        lib = _lib.load()
+        n = w.numel()
+        work = self._mdot_work[self.restart + 2:]
+        _lib.check(lib.tf_vec_mdot(n, k, V.data_ptr(), V.stride(0), w.data_ptr(), out.data_ptr(),
+                                   work.data_ptr(), work.numel() * 8, _stream()), 'tf_vec_mdot')
 
     def _mdot(self, V, k, w):
         lib = _lib.load()
@@ -208,6 +349,13 @@ class Solver:
         _lib.check(lib.tf_vec_mgs_update(w.numel(), k, V.data_ptr(), V.stride(0), h.data_ptr(), w.data_ptr(),
                                          _stream()), 'tf_vec_mgs_update')
 
+    def _copy(self, src, dst):
+        self._axpby(1.0, src, 0.0, None, dst)
+
+    def _zero(self, z):
+        lib = _lib.load()
+        _lib.check(lib.tf_vec_fill(z.numel(), 0.0, z.data_ptr(), _stream()), 'tf_vec_fill')
+
     def _axpby(self, a, x, b, y, z):
         lib = _lib.load()
         _lib.check(lib.tf_vec_axpby(z.numel(), float(a), None if x is None else x.data_ptr(), float(b),
@@ -217,20 +365,26 @@ class Solver:
         out = self._mdot(w.view(1, -1), 1, w)
         return math.sqrt(max(float(out.item()), 0.0))
 
-    def fgmres(self, fac, b):
-        """Solve A_g x = b (b: float64 CUDA tensor); returns (x, iterations, relres)."""
+    def fgmres(self, op, fac, b, maxit=None):
+        """Solve A_g x = b (b: float64 CUDA tensor) with preconditioner fac;
+        returns (x, iterations, relres)."""
+        maxit = self.maxit if maxit is None else maxit
+        import time
+        t_start = time.perf_counter()
         n = b.numel()
         V, Z = self._workspace(n, b.device)
         m = self.restart
-        x = torch.zeros_like(b)
-        r = b.clone()
+        x = torch.empty_like(b)
+        self._zero(x)
+        r = torch.empty_like(b)
+        self._copy(b, r)
         bn = self._norm(b)
         if bn == 0.0:
             return x, 0, 0.0
         its = 0
         relres = 1.0
         tmp = torch.empty_like(b)
-        while its < self.maxit:
+        while its < maxit:
             beta = self._norm(r)
             relres = beta / bn
             if relres <= self.tol:
@@ -243,15 +397,18 @@ class Solver:
             sn = np.zeros(m)
             k = 0
             for j in range(m):
-                Z[j].copy_(V[j])
+                self._copy(V[j], Z[j])
                 fac.apply(Z[j])
-                fac.matvec(Z[j], V[j + 1])
+                op.matvec(Z[j], V[j + 1])
                 w = V[j + 1]
-                h = self._mdot(V, j + 1, w).clone()
+                hbuf = self._hbuf[:2 * (j + 1)]
+                h, h2 = hbuf[:j + 1], hbuf[j + 1:]
+                self._mdot_into(V, j + 1, w, h)
                 self._mgs(V, j + 1, h, w)
-                h2 = self._mdot(V, j + 1, w)
+                self._mdot_into(V, j + 1, w, h2)
                 self._mgs(V, j + 1, h2, w)
-                hh = (h + h2).cpu().numpy()
+                hb = hbuf.cpu().numpy()
+                hh = hb[:j + 1] + hb[j + 1:]
                 hn = self._norm(w)
                 H[:j + 1, j] = hh
                 H[j + 1, j] = hn
@@ -270,35 +427,81 @@ class Solver:
                 g[j] = cs[j] * g[j]
                 its += 1
                 k = j + 1
-                if abs(g[j + 1]) <= self.tol * bn or its >= self.maxit or hn == 0:
+                if abs(g[j + 1]) <= self.tol * bn or its >= maxit or hn == 0:
                     break
             y = np.linalg.solve(np.triu(H[:k, :k]), g[:k]) if k else np.zeros(0)
-            yd = torch.as_tensor(y, dtype=torch.float64).to(b.device)
+            yd = torch.as_tensor(-y, dtype=torch.float64).to(b.device)
             # x += Z[:k]^T y
-            self._mgs(Z, k, -yd, x) if k else None
+            self._mgs(Z, k, yd, x) if k else None
             # true residual
-            fac.matvec(x, tmp)
+            op.matvec(x, tmp)
             self._axpby(1.0, b, -1.0, tmp, r)
         self.stats['gmres_iterations'] += its
         self.stats['last_relres'] = relres
+        if its:
+            self._cost_iter = self._ema(self._cost_iter, (time.perf_counter() - t_start) / its)
         return x, its, relres
 
     # -- the reference's solve contract ---------------------------------------
+    @staticmethod
+    def _ema(old, new):
+        return new if old is None else 0.7 * old + 0.3 * new
+
+    def _reuse_limit(self):
+        """GMRES iterations a reused factorisation may take before a fresh
+        factorisation would have been cheaper (at most reuse_maxit)."""
+        done = [(a, b) for a, b in self._pending if b.query()]
+        for a, b in done:
+            self._cost_factor = self._ema(self._cost_factor, a.elapsed_time(b) / 1000.0)
+        self._pending = [(a, b) for a, b in self._pending if (a, b) not in done]
+        if self.reuse_policy == 'always':
+            return self.reuse_maxit
+        if self._skip > 0:
+            # recent reuse attempts failed: back off before trying again
+            self._skip -= 1
+            return 0
+        if self._cost_factor is None or self._cost_iter is None:
+            return self.reuse_maxit
+        return int(min(self.reuse_maxit, self._cost_factor / self._cost_iter))
+
+    def _solve_gauged(self, op, b):
+        """x with A_g x = b to the tolerance, reusing the latest factorisation
+        as preconditioner while that is cheaper than refactoring."""
+        own = op.jac.lu
+        if isinstance(own, Factorization) and own.valid() and own.precision == self.precision:
+            return self.fgmres(op, own, b)
+        prec = self._prec
+        limit = self._reuse_limit() if self.reuse else 0
+        if limit >= 2 and prec is not None and prec.valid() and prec.precision == self.precision:
+            x, its, rr = self.fgmres(op, prec, b, maxit=limit)
+            if math.isfinite(rr) and rr <= self.tol:
+                self.stats['reused'] += 1
+                self._fail_streak = 0
+                return x, its, rr
+            self.stats['refactored_after_reuse'] += 1
+            self._fail_streak += 1
+            if self._fail_streak >= 2:
+                self._skip = 2 ** min(self._fail_streak, 6)
+        return self.fgmres(op, self.factorize(op), b)
+
     def solve(self, jac, rhs, rhs2=None, V=None, W=None, C=None):
         itf = self.itf
-        fac = self.factorization(jac)
+        op = self.operator(jac)
         self.stats['solves'] += 1
-        b = _to_tensor(rhs, itf.device).clone()
+        src = _to_tensor(rhs, itf.device)
+        b = torch.empty_like(src)
+        self._copy(src, b)
         if rhs2 is None:
             if self.gauge >= 0:
-                b[self.gauge] = 0.0
-            x, its, rr = self.fgmres(fac, b)
+                lib = _lib.load()
+                _lib.check(lib.tf_vec_fill(1, 0.0, b.data_ptr() + 8 * self.gauge, _stream()), 'tf_vec_fill')
+            x, its, rr = self._solve_gauged(op, b)
             if not math.isfinite(rr) or rr > max(self.tol, 1e-6):
                 raise RuntimeError('GMRES did not converge: relative residual %.3e after %d iterations' % (rr, its))
             return DeviceVector(x)
-        return self._bordered(fac, b, rhs2, V, W, C)
+        return self._bordered(op, b, rhs2, V, W, C)
 
-    def _bordered(self, fac, b, rhs2, V, W, C):
+    def _bordered(self, op, b, rhs2, V, W, C):
         """Block elimination of [A_g, sV; sW'^T, s^2 C][y; t] = [b; s rhs2], where
         W' is W without its gauge entry (SciPy.py:93-126) and b keeps its gauge
         entry (SciPy.py:226-227)."""
@@ -311,8 +514,8 @@ class Solver:
         if self.gauge >= 0:
             Wt[self.gauge] = 0.0
         Cv = 0.0 if C is None else float(C)
-        y0, i0, r0 = self.fgmres(fac, b.clone())
-        y1, i1, r1 = self.fgmres(fac, (s * Vt).contiguous())
+        y0, i0, r0 = self._solve_gauged(op, b.clone())
+        y1, i1, r1 = self._solve_gauged(op, (s * Vt).contiguous())
         if max(r0, r1) > max(self.tol, 1e-6):
             raise RuntimeError('GMRES did not converge in a bordered solve')
         wy0 = float(_dot_t(Wt, y0))
