@@ -57,15 +57,25 @@ def parse():
     ap.add_argument('--no-baseline', action='store_true')
     ap.add_argument('--profile', default=None, choices=['factor', 'solve', 'assemble'],
                     help='run only a few launches of one stage (for ncu captures)')
+    ap.add_argument('--nz', type=int, default=1, help='cells in z (1: the 2D grid)')
+    ap.add_argument('--batched', type=int, default=0,
+                    help='time this many random lid-driven cavities (nx from 32..192, Re from [100, 4000], '
+                         'seed 2) solved concurrently and one after the other, then exit')
+    ap.add_argument('--re', type=float, default=1000.0, help='Reynolds number of the --profile state')
     return ap.parse_args()
 
 
 def config(args):
-    return {'workload': '2D lid-driven cavity %dx%d, dof 3 (%d unknowns), Newton at Re=0 then continuation '
+    if args.nz > 1:
+        n = 4 * args.nx * args.nx * args.nz
+        grid = '3D lid-driven cavity %dx%dx%d, dof 4' % (args.nx, args.nx, args.nz)
+    else:
+        n = 3 * args.nx * args.nx
+        grid = '2D lid-driven cavity %dx%d, dof 3' % (args.nx, args.nx)
+    return {'workload': '%s (%d unknowns), Newton at Re=0 then continuation '
                         'Re 0->%g, ds=%g, ||F||<=1e-8, FP64 GMRES to %g + ND-LU (%s factors)'
-                        % (args.nx, args.nx, 3 * args.nx * args.nx, args.target, args.ds, args.tol,
-                           args.precision),
-            'nx': args.nx, 'ny': args.nx, 'dof': 3, 'unknowns': 3 * args.nx * args.nx,
+                        % (grid, n, args.target, args.ds, args.tol, args.precision),
+            'nx': args.nx, 'ny': args.nx, 'nz': args.nz, 'dof': 4 if args.nz > 1 else 3, 'unknowns': n,
             'target_re': args.target, 'ds': args.ds, 'newton_tolerance': 1e-8,
             'l2': 'working set larger than L2 (1.1 GB of frontal matrices at 256^2)',
             'parallelism': 'replicas (one instance per GPU)'}
@@ -142,7 +152,7 @@ def gpu_arm(args, rank, world, local):
     torch.cuda.set_device(local)
     lib = _lib.load()
     params = {'CUDA': {'Factor Precision': args.precision, 'Tolerance': args.tol}}
-    itf = Interface(params, args.nx, args.nx)
+    itf = Interface(params, args.nx, args.nx, args.nz)
     n = itf.n
     stream = torch.cuda.current_stream()
 
@@ -402,17 +412,26 @@ def reference_arm(args, rank):
 
 def profile_stage(args):
     """A short, fixed sequence of one stage for profiler captures: the
-    Jacobian of a converged-like state at Re = 1000, then 3 factorisations,
-    3 preconditioner applications or 3 fused assemblies."""
+    Jacobian of a random state (Re from --re, 2D unless --nz > 1), then 3
+    factorisations, 3 preconditioner applications or 3 fused assemblies,
+    each timed with CUDA events on the launching stream."""
     import torch
     from transiflow_gb300 import Interface
-    p = {'Reynolds Number': 1000.0, 'CUDA': {'Factor Precision': args.precision, 'CUDA Graphs': False}}
-    itf = Interface(p, args.nx, args.nx)
+    p = {'Reynolds Number': args.re, 'CUDA': {'Factor Precision': args.precision, 'CUDA Graphs': False}}
+    itf = Interface(p, args.nx, args.nx, args.nz)
     s = 0.1 * np.random.default_rng(1).standard_normal(itf.n)
     x = itf.vector_from_array(s)
     J = itf.jacobian(x)
+    t0 = time.perf_counter()
     fac = itf.solver.factorization(J)
+    torch.cuda.synchronize()
+    first = time.perf_counter() - t0
+    st = torch.cuda.current_stream()
+    times = []
     for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
         if args.profile == 'factor':
             J.lu = None
             fac = itf.solver.factorization(J)
@@ -421,14 +440,50 @@ def profile_stage(args):
         else:
             itf.rhs(x)
             itf.jacobian(x)
+        e1.record(st)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1000.0)
+    plan = itf.solver.plan
+    print(json.dumps({'profile': args.profile, 'nx': args.nx, 'nz': args.nz, 'unknowns': itf.n,
+                      'precision': args.precision, 's_per_call': times, 'first_factor_s': first,
+                      'factor_gflop': plan.flops / 1e9, 'front_gb': plan.front_elems * (8 if args.precision == 'fp64' else 4) / 1e9}))
+
+
+def batched(args):
+    """The batched configuration: many independent lid-driven cavities of
+    uneven size and Reynolds number, each by Newton at Re = 0 and continuation
+    to its Re with ||F|| <= 1e-10, solved concurrently (one stream per
+    instance) and one after the other on the same GPU."""
+    import torch
+    from transiflow_gb300.batch import solve_instance, solve_many
+    rng = np.random.default_rng(2)
+    specs = [{'nx': int(rng.choice(np.arange(32, 193, 16))), 'target': float(rng.uniform(100, 4000)),
+              'ds': 200.0, 'tolerance': 1e-10} for _ in range(args.batched)]
+    solve_many(specs[:4])                      # plans and kernels warm
+    for sp in {s['nx']: s for s in specs}.values():
+        solve_instance(dict(sp, target=100.0))  # every grid shape's plan built before timing
     torch.cuda.synchronize()
-    print(json.dumps({'profile': args.profile, 'nx': args.nx, 'precision': args.precision}))
+    t0 = time.perf_counter()
+    res = solve_many(specs)
+    torch.cuda.synchronize()
+    t_conc = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for sp in specs:
+        solve_instance(sp)
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    print(json.dumps({'batched': args.batched, 'concurrent_s': t_conc, 'sequential_s': t_seq,
+                      'max_fnorm': max(r['fnorm'] for r in res),
+                      'unknowns': int(sum(3 * s['nx'] ** 2 for s in specs))}))
 
 
 def main():
     args = parse()
     if args.profile:
         profile_stage(args)
+        return
+    if args.batched:
+        batched(args)
         return
     from transiflow_gb300 import dist
     rank, world, local = dist.init_from_env()

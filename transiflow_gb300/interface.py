@@ -19,14 +19,21 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
   'Reuse Factorization'  precondition a new Jacobian with the latest
                       factorisation and refactor only if GMRES needs more than
                       'Reuse Iterations' (default 20) iterations (default True)
-  'Reuse Policy'      'cost' (default): reuse only while the extra GMRES
-                      iterations cost less than a factorisation (measured),
-                      backing off after failed attempts; 'always'
+  'Reuse Policy'      'cost' (default): try a reuse only while the Jacobian
+                      values differ from the factored ones by at most
+                      'Reuse Drift' (relative 2-norm, default 0.05; halved
+                      after a failed attempt, grown after a success) and with
+                      at most as many GMRES iterations as cost one
+                      factorisation (both measured); 'always'
   'CUDA Graphs'       replay the factorisation and solve launch sequences from
                       captured CUDA graphs (default True)
   'Fuse Jacobian'     compute the Jacobian together with the RHS and reuse it
                       when jacobian() is called at the same state and
                       parameters (default False)
+With the reference's ``'Use Iterative Solver': True``, the GMRES restart,
+iteration cap and tolerance come from its ``'Iterative Solver'`` dictionary
+('Restart' 100, 'Maximum Iterations' 1000, 'Convergence Tolerance' 1e-6 by
+default, as in SciPy.py:281-287); the preconditioner stays the LU above.
 """
 
 import ctypes
@@ -98,13 +105,20 @@ class Interface:
                    'tf_stencil_pattern')
         self.pattern = Pattern(rowptr, cols, self.n, width, row_offset, slot.reshape(self.dof, self.dof, 27))
         opts = parameters.get('CUDA', {})
-        self.solver = Solver(self, restart=opts.get('Restart', 50), tol=opts.get('Tolerance', 1e-12),
-                             maxit=opts.get('Maximum Iterations', 500),
+        restart, tol, maxit = opts.get('Restart', 50), opts.get('Tolerance', 1e-12), opts.get('Maximum Iterations', 500)
+        if parameters.get('Use Iterative Solver', False):
+            # the reference's GMRES settings (SciPy.py:281-287) take precedence
+            it = parameters.get('Iterative Solver', {})
+            restart = it.get('Restart', 100)
+            maxit = it.get('Maximum Iterations', 1000)
+            tol = it.get('Convergence Tolerance', 1e-6)
+        self.solver = Solver(self, restart=restart, tol=tol, maxit=maxit,
                              precision=opts.get('Factor Precision', 'fp64'),
                              reuse=opts.get('Reuse Factorization', True),
                              reuse_maxit=opts.get('Reuse Iterations', 20),
                              graphs=opts.get('CUDA Graphs', True),
-                             reuse_policy=opts.get('Reuse Policy', 'cost'))
+                             reuse_policy=opts.get('Reuse Policy', 'cost'),
+                             reuse_drift=opts.get('Reuse Drift', 0.05))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

@@ -16,6 +16,7 @@ with two solves of the gauged Jacobian.
 """
 
 import math
+import threading
 
 import numpy as np
 import torch
@@ -28,6 +29,7 @@ from .vector import DeviceVector, _stream
 # Elimination plans depend only on the grid shape and the variables, so
 # interfaces of the same shape share one (keyed by shape and device).
 _PLANS = {}
+_PLANS_LOCK = threading.Lock()
 
 
 class NdPlanDevice:
@@ -147,8 +149,13 @@ class _Graphed:
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         before = lib.tf_launch_count()
+        # capture on this thread's stream unless it is the default stream
+        # (torch's shared side stream is then used), so that threads driving
+        # instances on their own streams can capture concurrently
+        cur = torch.cuda.current_stream()
+        kw = {} if cur == torch.cuda.default_stream() else {'stream': cur}
         try:
-            with torch.cuda.graph(g, capture_error_mode='thread_local'):
+            with torch.cuda.graph(g, capture_error_mode='thread_local', **kw):
                 self.fn()
         except RuntimeError:
             self.failed = True
@@ -225,7 +232,7 @@ class Solver:
     """Per-interface solver state: the plan, factor buffers, Krylov workspace."""
 
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
-                 reuse_maxit=20, graphs=True, reuse_policy='cost'):
+                 reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05):
         self.itf = interface
         self.graphs = graphs
         self._engines = {}
@@ -237,8 +244,10 @@ class Solver:
         self._cost_iter = None
         self._pending = []
         self.reuse_policy = reuse_policy
-        self._fail_streak = 0
-        self._skip = 0
+        # relative change of the Jacobian values up to which a reuse is tried;
+        # adapted: halved after a failed attempt, grown after a success
+        self._drift_tol = reuse_drift
+        self._drift_work = None
         self.gauge = interface.pressure_row if interface.dof > interface.dim else -1
         self.restart = restart
         self.tol = tol
@@ -259,10 +268,11 @@ class Solver:
             itf = self.itf
             pvar = itf.dim if itf.dof > itf.dim else None
             key = (itf.nx, itf.ny, itf.nz, itf.dim, itf.dof, pvar, str(pattern.rowptr.device))
-            plan = _PLANS.get(key)
-            if plan is None:
-                plan = NdPlanDevice(pattern, itf.nx, itf.ny, itf.nz, itf.dof, pvar)
-                _PLANS[key] = plan
+            with _PLANS_LOCK:
+                plan = _PLANS.get(key)
+                if plan is None:
+                    plan = NdPlanDevice(pattern, itf.nx, itf.ny, itf.nz, itf.dof, pvar)
+                    _PLANS[key] = plan
             self.plan = plan
             self.info = torch.zeros(1, dtype=torch.int32, device=pattern.rowptr.device)
 
@@ -325,7 +335,7 @@ class Solver:
             lib = _lib.load()
             wb = lib.tf_vec_mdot_workspace_bytes(n, m + 1)
             self._mdot_work = torch.empty((wb + 7) // 8 + m + 2, dtype=torch.float64, device=dev)
-            self._hbuf = torch.empty(2 * (m + 1), dtype=torch.float64, device=dev)
+            self._hbuf = torch.empty(2 * (m + 1) + 1, dtype=torch.float64, device=dev)
         return self._V, self._Z
 
     def _mdot_into(self, V, k, w, out):
@@ -370,7 +380,6 @@ class Solver:
         returns (x, iterations, relres)."""
         maxit = self.maxit if maxit is None else maxit
         import time
-        t_start = time.perf_counter()
         n = b.numel()
         V, Z = self._workspace(n, b.device)
         m = self.restart
@@ -379,6 +388,9 @@ class Solver:
         r = torch.empty_like(b)
         self._copy(b, r)
         bn = self._norm(b)
+        # the norm synchronises: work queued before this solve (a
+        # factorisation) is not charged to the iterations
+        t_start = time.perf_counter()
         if bn == 0.0:
             return x, 0, 0.0
         its = 0
@@ -401,15 +413,17 @@ class Solver:
                 fac.apply(Z[j])
                 op.matvec(Z[j], V[j + 1])
                 w = V[j + 1]
-                hbuf = self._hbuf[:2 * (j + 1)]
-                h, h2 = hbuf[:j + 1], hbuf[j + 1:]
+                # CGS2 and the new vector's norm, read back with one sync
+                hbuf = self._hbuf[:2 * (j + 1) + 1]
+                h, h2, ww = hbuf[:j + 1], hbuf[j + 1:2 * (j + 1)], hbuf[2 * (j + 1):]
                 self._mdot_into(V, j + 1, w, h)
                 self._mgs(V, j + 1, h, w)
                 self._mdot_into(V, j + 1, w, h2)
                 self._mgs(V, j + 1, h2, w)
+                self._mdot_into(w.view(1, -1), 1, w, ww)
                 hb = hbuf.cpu().numpy()
-                hh = hb[:j + 1] + hb[j + 1:]
-                hn = self._norm(w)
+                hh = hb[:j + 1] + hb[j + 1:2 * (j + 1)]
+                hn = math.sqrt(max(float(hb[-1]), 0.0))
                 H[:j + 1, j] = hh
                 H[j + 1, j] = hn
                 if hn > 0:
@@ -456,10 +470,6 @@ class Solver:
         self._pending = [(a, b) for a, b in self._pending if (a, b) not in done]
         if self.reuse_policy == 'always':
             return self.reuse_maxit
-        if self._skip > 0:
-            # recent reuse attempts failed: back off before trying again
-            self._skip -= 1
-            return 0
         if self._cost_factor is None or self._cost_iter is None:
             return self.reuse_maxit
         return int(min(self.reuse_maxit, self._cost_factor / self._cost_iter))
@@ -473,16 +483,35 @@ class Solver:
         prec = self._prec
         limit = self._reuse_limit() if self.reuse else 0
         if limit >= 2 and prec is not None and prec.valid() and prec.precision == self.precision:
-            x, its, rr = self.fgmres(op, prec, b, maxit=limit)
-            if math.isfinite(rr) and rr <= self.tol:
-                self.stats['reused'] += 1
-                self._fail_streak = 0
-                return x, its, rr
-            self.stats['refactored_after_reuse'] += 1
-            self._fail_streak += 1
-            if self._fail_streak >= 2:
-                self._skip = 2 ** min(self._fail_streak, 6)
+            if self.reuse_policy == 'always' or self._drift(op) <= self._drift_tol:
+                x, its, rr = self.fgmres(op, prec, b, maxit=limit)
+                if math.isfinite(rr) and rr <= self.tol:
+                    self.stats['reused'] += 1
+                    self._drift_tol = min(0.5, 1.25 * self._drift_tol)
+                    return x, its, rr
+                self.stats['refactored_after_reuse'] += 1
+                self._drift_tol *= 0.5
         return self.fgmres(op, self.factorize(op), b)
+
+    def _drift(self, op):
+        """||A_new - A_f|| / ||A_f|| over the stencil values, A_f being the
+        operator of the latest factorisation (its values are still in the
+        engine's staging buffer)."""
+        lib = _lib.load()
+        eng = self._engine(self.precision)
+        m = op.values.numel()
+        if self._drift_work is None or self._drift_work[0].numel() != m:
+            wb = lib.tf_vec_mdot_workspace_bytes(m, 1)
+            self._drift_work = (torch.empty(m, dtype=torch.float64, device=op.values.device),
+                                torch.empty((wb + 7) // 8, dtype=torch.float64, device=op.values.device),
+                                torch.empty(2, dtype=torch.float64, device=op.values.device))
+        d, work, out = self._drift_work
+        self._axpby(1.0, op.values, -1.0, eng.staging, d)
+        for v, o in ((d, out[0:1]), (eng.staging, out[1:2])):
+            _lib.check(lib.tf_vec_mdot(m, 1, v.data_ptr(), m, v.data_ptr(), o.data_ptr(), work.data_ptr(),
+                                       work.numel() * 8, _stream()), 'tf_vec_mdot')
+        dn, fn = out.cpu().numpy()
+        return math.sqrt(max(dn, 0.0) / fn) if fn > 0 else math.inf
 
     def solve(self, jac, rhs, rhs2=None, V=None, W=None, C=None):
         itf = self.itf
