@@ -366,11 +366,16 @@ def oracle_sample(nx, seed=1):
 # Call counts of the branch (2D LDC 256^2, Re 0 -> 5000, ds = 200,
 # newton_tolerance 1e-8) as run by the continuation driver; the GPU arm
 # recomputes them live and the reference arm uses these.
-BRANCH_CALLS_256 = {'rhs': None, 'jacobian': None, 'solve': None, 'factorizations': None}
+# Interface calls of the 256^2 branch (Re 0 -> 5000, ds = 200, ||F|| <= 1e-8) as
+# the reference's Continuation makes them on an exact solver; the SciPy
+# interface factors every Jacobian once (the LU is cached on the matrix).
+BRANCH_CALLS_256 = {'rhs': 111, 'jacobian': 47, 'solve': 92, 'factorizations': 47}
 
 
 def extrapolate(t, calls):
-    nfac = calls.get('factorizations') or calls['jacobian']
+    """Seconds of the reference's SciPy path for these call counts: one
+    SuperLU factorisation per Jacobian (SciPy.py:151, cached on the matrix)."""
+    nfac = calls['jacobian']
     return (calls['rhs'] * t['rhs'] + calls['jacobian'] * t['jacobian'] + nfac * t['factor_solve']
             + max(calls['solve'] - nfac, 0) * t['solve'])
 
@@ -381,9 +386,9 @@ def cpu_baseline(args, calls):
     return {'value': est, 'unit': 's', 'cores': 1, 'kind': 'port',
             'sample': 'oracle (vectorised NumPy restatement of Discretization + SciPy SuperLU, '
                       'single-threaded splu) at %dx%d: 1 rhs %.2fs, 1 jacobian %.2fs, 1 factor+solve %.2fs, '
-                      '1 solve %.2fs, scaled by the branch call counts %s'
+                      '1 solve %.2fs, scaled by the branch call counts %s (one factorisation per jacobian)'
                       % (args.nx, args.nx, t['rhs'], t['jacobian'], t['factor_solve'], t['solve'],
-                         {k: calls[k] for k in ('rhs', 'jacobian', 'solve', 'factorizations')}),
+                         {k: calls[k] for k in ('rhs', 'jacobian', 'solve')}),
             'host_cpus': os.cpu_count()}
 
 
@@ -391,8 +396,8 @@ def reference_arm(args, rank):
     if rank != 0:
         return None
     calls = dict(BRANCH_CALLS_256)
-    if any(v is None for v in calls.values()):
-        calls = {'rhs': 120, 'jacobian': 51, 'solve': 100, 'factorizations': 51}
+    if args.nx != 256 or args.nz != 1:
+        return {'impl': 'reference', 'unavailable': 'branch call counts are known for the 256x256 branch only'}
     for _ in range(args.warmup):
         oracle_sample(args.nx)
     vals = []

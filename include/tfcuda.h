@@ -95,6 +95,16 @@ typedef struct tf_problem {
     int32_t metric_stride;
     int32_t nops;
     tf_bc_op ops[TF_MAX_BC_OPS];
+    /* beta-plane Coriolis term and wind stress (2D; Discretization.py:253-255,
+     * 1086-1118): rossby = 'Rossby Parameter' (0: no Coriolis term), wind =
+     * 'Wind Stress Parameter' / (2 pi) (0: no wind forcing), asym = 'Asymmetry
+     * Parameter'.  d_aux: device pointer to double[4][ny] with, for row j of
+     * face coordinates y: y[j]/2, -(y[j]+y[j-1])/4, cos(2 pi yc), cos(pi yc),
+     * yc = (y[j]+y[j-1])/2; may be NULL when rossby == wind == 0.             */
+    double rossby;
+    double wind;
+    double asym;
+    const double *d_aux;
 } tf_problem;
 
 /* ---- library ------------------------------------------------------------*/

@@ -275,7 +275,7 @@ class Discretization:
                 dof = self.dim + 3
         self.dof = dof
         if self.problem not in ('lid-driven cavity', 'differentially heated cavity',
-                                'rayleigh-benard', 'rayleigh-benard perturbation'):
+                                'rayleigh-benard', 'rayleigh-benard perturbation', 'double gyre'):
             raise NotImplementedError('problem type %s' % self.problem)
         self.zper = nz == 1
         p = parameters
@@ -329,8 +329,9 @@ class Discretization:
         Ra = self.get_parameter('Rayleigh Number', 1.0)
         Pr = self.get_parameter('Prandtl Number', 1.0)
         Gr = self.get_parameter('Grashof Number', Ra / Pr)
-        if self.get_parameter('Rossby Parameter'):
-            raise NotImplementedError('Coriolis term')
+        beta = self.get_parameter('Rossby Parameter')
+        if beta and dim != 2:
+            raise NotImplementedError('Coriolis term in 3D')
         if Re == 0:
             Re = 1
         if Gr == 0:
@@ -346,6 +347,8 @@ class Discretization:
         v_y = self._line(dim, 1, 1, {0: -(Dx * Dz), 1: Dx * Dz})
         if dim == 2:
             atom = 1 / (Re * np.sqrt(Gr)) * (u_xx + u_yy + v_xx + v_yy) - (p_x + p_y) + (u_x + v_y)
+            if beta:
+                atom -= beta * self.coriolis()
             if dof > 3:
                 T = dim + 1
                 atom += 1 / (Pr * np.sqrt(Gr)) * (self._second(T, T, 0, Hx, Hpx, Dy, Dz)
@@ -392,6 +395,43 @@ class Discretization:
                 ba = Hpy * Dx * Dz / 2
                 atom += Bi / (Bi + 1) * self._line(dim + 1, 1, 1, {0: ba, 1: ba})
         return atom
+
+    def coriolis(self):
+        """Discretization.coriolis, Discretization.py:1086-1099: beta-plane
+        Coriolis couplings, y v averaged to u points and y u to v points."""
+        g = self._geo()
+        yj = _b3y(self.y[:self.ny])
+        yjm = _b3y(self.y[np.arange(self.ny) - 1])
+        a = self._atom()
+        shape = (self.nx, self.ny, self.nz)
+        cv = (g['Hpy'] * g['Dx'] * g['Dz'] / 2) * (yj / 2)       # v row, u at x-1/0, y 0/+1
+        cu = (g['Hpx'] * g['Dy'] * g['Dz'] / 2) * (-(yj + yjm) / 4)   # u row, v at x 0/+1, y -1/0
+        for ox in (0, 1):
+            for oy in (1, 2):
+                a[:, :, :, 1, 0, ox, oy, 1] = np.broadcast_to(cv, shape)
+        for ox in (1, 2):
+            for oy in (0, 1):
+                a[:, :, :, 0, 1, ox, oy, 1] = np.broadcast_to(cu, shape)
+        return a
+
+    def wind_stress(self):
+        """Discretization.wind_stress, Discretization.py:1101-1118: zonal
+        wind forcing of the u equation (not on the east wall)."""
+        alpha = self.get_parameter('Wind Stress Parameter')
+        asym = self.get_parameter('Asymmetry Parameter')
+        frc = np.zeros((self.nx, self.ny, self.nz, self.dof))
+        x, y, z = self.x, self.y, self.z
+        i = np.arange(self.nx - 1)[:, None, None]
+        j = np.arange(self.ny)[None, :, None]
+        k = np.arange(self.nz)[None, None, :]
+        dx = (x[i + 1] - x[i - 1]) / 2
+        dy = y[j] - y[j - 1]
+        dz = z[k] - z[k - 1]
+        yc = (y[j] + y[j - 1]) / 2
+        f = - (1 - asym) * np.cos(2 * np.pi * yc) - asym * np.cos(np.pi * yc)
+        f = f * (alpha / (2 * np.pi) * dx * dy * dz)
+        frc[:self.nx - 1, :, :, 0] = f
+        return frc
 
     # -- nonlinear part (Discretization.py:319-365, 1178-1467) -----------------
 
@@ -619,6 +659,11 @@ class Discretization:
             temperature(2, False, bottom)
             wall(2, True, +1)
             wall(2, False)
+        elif p == 'double gyre':
+            wall(0, True)
+            wall(0, False)
+            wall(1, True, +1)
+            wall(1, False, +1)
         elif p == 'differentially heated cavity':
             temperature(0, True, -1 / 2)
             temperature(0, False, 1 / 2)
@@ -637,7 +682,10 @@ class Discretization:
 
     def boundaries(self, atom):
         """Discretization.boundaries, Discretization.py:704-714."""
-        frc = np.zeros((self.nx, self.ny, self.nz, self.dof))
+        if self.problem == 'double gyre':
+            frc = self.wind_stress()
+        else:
+            frc = np.zeros((self.nx, self.ny, self.nz, self.dof))
         for op in self.bc_program():
             if op[0] == 'wall':
                 apply_wall(atom, frc, op[1], op[2], op[3])

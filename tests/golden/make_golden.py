@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this directory by running the reference.
 
 Usage (needs the reference checkout, which only this container has):
-    PYTHONPATH=/root/reference python tests/golden/make_golden.py
+    PYTHONPATH=/root/reference python tests/golden/make_golden.py [fixture names]
 
 Every fixture is computed by the reference itself (BIMAU/transiflow 1.0.1):
 ``transiflow.Discretization`` for RHS / Jacobian / mass matrix,
@@ -49,6 +49,11 @@ CASES = [
     ('rbp2d_6x5', {'Reynolds Number': 1, 'Rayleigh Number': 1000, 'Prandtl Number': 10,
                    'Problem Type': 'Rayleigh-Benard Perturbation', 'Biot Number': 0.5},
      6, 5, 1, None, None, ('normal', 5, 1)),
+    ('qg2d_4_ramp', {'Reynolds Number': 16, 'Rossby Parameter': 1000, 'Wind Stress Parameter': 1000,
+                     'Problem Type': 'Double Gyre'}, 4, 4, 1, 2, 4, ('ramp',)),
+    ('qg2d_8x6', {'Reynolds Number': 30, 'Rossby Parameter': 500, 'Wind Stress Parameter': 700,
+                  'Asymmetry Parameter': 0.3, 'Problem Type': 'Double Gyre'}, 8, 6, 1, None, None,
+     ('normal', 6, 2)),
 ]
 
 
@@ -118,15 +123,20 @@ def branch_fixture():
                         X=np.array([p[1] for p in pts]), x0=np.array(x0))
 
 
-def main():
+def main(names=None):
+    """Write every fixture, or only the named ones."""
     for case in CASES:
+        if names and case[0] not in names:
+            continue
         discretization_fixture(*case)
         print('wrote', case[0])
-    solve_fixture()
-    print('wrote solve_ldc2d_12')
-    branch_fixture()
-    print('wrote branch_ldc2d_16')
+    if not names or 'solve_ldc2d_12' in names:
+        solve_fixture()
+        print('wrote solve_ldc2d_12')
+    if not names or 'branch_ldc2d_16' in names:
+        branch_fixture()
+        print('wrote branch_ldc2d_16')
 
 
 if __name__ == '__main__':
-    main()
+    main(sys.argv[1:])

@@ -147,3 +147,24 @@ def test_graph_replay_matches_eager_launches():
     for ya, yb in zip(out[False][0], out[True][0]):
         assert np.linalg.norm(ya - yb) <= 1e-10 * np.linalg.norm(ya)
     assert out[True][1] > 0 and out[False][1] == 0
+
+
+QG = {'Problem Type': 'Double Gyre', 'Reynolds Number': 16, 'Rossby Parameter': 1000,
+      'Wind Stress Parameter': 0}
+
+
+def test_double_gyre_wind_branch_matches_oracle():
+    """The reference's double-gyre continuation (test_continuation.py:400-416):
+    wind stress 0 -> 1000 at Re = 16, beta = 1000; every accepted point is a
+    root of the oracle's equations too."""
+    from transiflow_gb300 import Interface
+    itf = Interface(dict(QG), 16, 16)
+    pts = _branch(itf, 'Wind Stress Parameter', 0.0, 1000.0, 200.0)
+    assert abs(pts[-1][0] - 1000.0) < 1e-3
+    assert np.linalg.norm(pts[-1][1]) > 0
+    for mu, x in pts[1:]:
+        itf.set_parameter('Wind Stress Parameter', mu)
+        assert itf.rhs(itf.vector_from_array(x)).norm() <= 1e-8
+        xg = _gpu_root(itf, 'Wind Stress Parameter', mu, x)
+        xr = _oracle_root(QG, (16, 16), 'Wind Stress Parameter', mu, x)
+        assert np.linalg.norm(xg - xr) <= 1e-8 * np.linalg.norm(xr)

@@ -68,6 +68,10 @@ LAYOUT_CASES = [
     (3, 4, {'Reynolds Number': 100}, (5, 4, 1)),
     (3, 5, {'Problem Type': 'Rayleigh-Benard', 'Rayleigh Number': 1e3, 'Reynolds Number': 1}, (4, 4, 3)),
     (3, 5, {'Problem Type': 'Rayleigh-Benard Perturbation', 'Biot Number': 0.3, 'Reynolds Number': 1}, (4, 4, 3)),
+    (2, 3, {'Problem Type': 'Double Gyre', 'Reynolds Number': 30, 'Rossby Parameter': 500,
+            'Wind Stress Parameter': 700}, (7, 6, 1)),
+    (2, 4, {'Problem Type': 'Double Gyre', 'Reynolds Number': 16, 'Rossby Parameter': 1000,
+            'Wind Stress Parameter': 1000}, (5, 6, 1)),
 ]
 
 

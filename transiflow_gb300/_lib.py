@@ -20,7 +20,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), 'include')
 
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 # the assembly TU keeps the reference's separate multiply/add rounding
-SOURCES = [('tf_assemble.cu', ['-fmad=false']), ('tf_sparse.cu', []), ('tf_nd.cu', [])]
+SOURCES = [('tf_assemble.cu', ['-fmad=false']), ('tf_sparse.cu', []), ('tf_nd.cu', []), ('tf_nd_panel_f32.cu', []),
+           ('tf_nd_panel_f64.cu', [])]
 
 TF_MAX_BC_OPS = 24
 TF_METRIC_FIELDS = 10
@@ -74,7 +75,9 @@ class Problem(ctypes.Structure):
                 ('buoy_row', ctypes.c_int32), ('biot_row', ctypes.c_int32),
                 ('visc', ctypes.c_double), ('cond', ctypes.c_double), ('biot', ctypes.c_double),
                 ('d_metric', ctypes.c_void_p), ('metric_stride', ctypes.c_int32),
-                ('nops', ctypes.c_int32), ('ops', BcOp * TF_MAX_BC_OPS)]
+                ('nops', ctypes.c_int32), ('ops', BcOp * TF_MAX_BC_OPS),
+                ('rossby', ctypes.c_double), ('wind', ctypes.c_double), ('asym', ctypes.c_double),
+                ('d_aux', ctypes.c_void_p)]
 
 
 class NdPlan(ctypes.Structure):

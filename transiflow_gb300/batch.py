@@ -14,8 +14,6 @@ its own stream.  Elimination plans are shared between instances of the same
 grid shape.
 """
 
-import contextlib
-import io
 import threading
 
 import torch
@@ -43,12 +41,11 @@ def solve_instance(spec, stream=None):
         tol = float(spec.get('tolerance', 1e-10))
         params[name] = start
         itf = Interface(params, spec['nx'], spec.get('ny', spec['nx']), spec.get('nz', 1))
-        cont = Continuation(itf, newton_tolerance=tol)
-        with contextlib.redirect_stdout(io.StringIO()):
-            x = cont.newton(itf.vector(), tol=tol)
-            mu = start
-            if target != start:
-                x, mu = cont.continuation(x, name, start, target, float(spec.get('ds', 100.0)))
+        cont = Continuation(itf, newton_tolerance=tol, quiet=True)
+        x = cont.newton(itf.vector(), tol=tol)
+        mu = start
+        if target != start:
+            x, mu = cont.continuation(x, name, start, target, float(spec.get('ds', 100.0)))
         itf.set_parameter(name, mu)
         fnorm = itf.rhs(x).norm()
         out = itf.array_from_vector(x)

@@ -51,8 +51,9 @@ class Continuation:
     def __init__(self, interface, delta=1.0, destination_tolerance=1e-4,
                  newton_tolerance=1e-4, maximum_newton_iterations=10,
                  optimal_newton_iterations=3, residual_check='F',
-                 bordered_solver=False, verbose=False, predictor=None, log=None):
+                 bordered_solver=False, verbose=False, predictor=None, log=None, quiet=False):
         self.interface = interface
+        self.quiet = quiet
         self.verbose = verbose
         self.destination_tolerance = destination_tolerance
         self.delta = delta
@@ -68,6 +69,12 @@ class Continuation:
         self.stats = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'points': 0,
                       'failed_correctors': 0, 'learned_accepted': 0, 'learned_rejected': 0}
         self._t0 = None
+
+    def _say(self, *args, **kwargs):
+        """The reference's progress messages; quiet=True drops them (threads
+        driving instances concurrently cannot redirect a shared stdout)."""
+        if not self.quiet:
+            print(*args, **kwargs)
 
     # -- counted interface calls ---------------------------------------------
     def _rhs(self, x):
@@ -91,7 +98,7 @@ class Continuation:
             if self.residual_check == 'F' or self.verbose:
                 fnorm = norm(fval)
             if self.residual_check == 'F' and fnorm < tol:
-                print('Newton converged in %d iterations with ||F||=%e' % (k, fnorm), flush=True)
+                self._say('Newton converged in %d iterations with ||F||=%e' % (k, fnorm), flush=True)
                 break
             jac = self._jac(x)
             dx = self._solve(jac, -fval)
@@ -99,10 +106,10 @@ class Continuation:
             if self.residual_check != 'F' or self.verbose:
                 dxnorm = norm(dx)
             if self.residual_check != 'F' and dxnorm < tol:
-                print('Newton converged in %d iterations with ||dx||=%e' % (k, dxnorm), flush=True)
+                self._say('Newton converged in %d iterations with ||dx||=%e' % (k, dxnorm), flush=True)
                 break
             if self.verbose:
-                print('Newton status at iteration %d: ||F||=%e, ||dx||=%e' % (k, fnorm, dxnorm), flush=True)
+                self._say('Newton status at iteration %d: ||F||=%e, ||dx||=%e' % (k, fnorm, dxnorm), flush=True)
         self.newton_iterations = k
         return x
 
@@ -120,7 +127,7 @@ class Continuation:
                 fnorm = norm(fval)
                 self._last_fnorm = fnorm
             if self.residual_check == 'F' and fnorm < self.newton_tolerance:
-                print('Newton corrector converged in %d iterations with ||F||=%e' % (k, fnorm), flush=True)
+                self._say('Newton corrector converged in %d iterations with ||F||=%e' % (k, fnorm), flush=True)
                 break
             if self.residual_check == 'F' and prev_norm is not None and prev_norm < fnorm:
                 self.newton_iterations = self.maximum_newton_iterations
@@ -147,15 +154,15 @@ class Continuation:
                 prev_norm = dxnorm
                 dxnorm = norm(dx)
             if self.residual_check != 'F' and dxnorm < self.newton_tolerance:
-                print('Newton corrector converged in %d iterations with ||dx||=%e' % (k, dxnorm), flush=True)
+                self._say('Newton corrector converged in %d iterations with ||dx||=%e' % (k, dxnorm), flush=True)
                 break
             if self.verbose:
-                print('Newton corrector status at iteration %d: ||F||=%e, ||dx||=%e' % (k, fnorm, dxnorm), flush=True)
+                self._say('Newton corrector status at iteration %d: ||F||=%e, ||dx||=%e' % (k, fnorm, dxnorm), flush=True)
             if self.residual_check != 'F' and prev_norm is not None and prev_norm < dxnorm:
                 self.newton_iterations = self.maximum_newton_iterations
                 break
         if self.newton_iterations == self.maximum_newton_iterations:
-            print('Newton did not converge. Adjusting step size and trying again', flush=True)
+            self._say('Newton did not converge. Adjusting step size and trying again', flush=True)
             self.stats['failed_correctors'] += 1
             return x0, mu0
         self.interface.set_parameter(name, mu)
@@ -168,7 +175,7 @@ class Continuation:
         ds *= factor
         ds = math.copysign(min(max(abs(ds), ds_min), ds_max), ds)
         if self.verbose:
-            print('New stepsize: ds=%e, factor=%e' % (ds, factor), flush=True)
+            self._say('New stepsize: ds=%e, factor=%e' % (ds, factor), flush=True)
         return ds
 
     # -- converge onto the target (Continuation.py:234-249) -------------------
@@ -176,7 +183,7 @@ class Continuation:
         for _ in range(maxit):
             if abs(target - mu) < self.destination_tolerance:
                 self.interface.set_parameter(name, target)
-                print("Convergence achieved onto target %s = %f" % (name, mu), flush=True)
+                self._say("Convergence achieved onto target %s = %f" % (name, mu), flush=True)
                 break
             ds = 1 / dmu * (target - mu)
             x, mu, dx, dmu, ds = self._step(name, x, mu, dx, dmu, ds, ds_min, ds_max)
@@ -207,7 +214,7 @@ class Continuation:
             if prev_ds == ds:
                 raise Exception('Newton cannot achieve convergence')
             return self._step(name, x0, mu0, dx, dmu, ds, ds_min, ds_max)
-        print("%s: %f" % (name, mu), flush=True)
+        self._say("%s: %f" % (name, mu), flush=True)
         self.stats['points'] += 1
         if self.log is not None:
             self.log({'mu': mu, 'fnorm': self._last_fnorm, 'newton_iterations': self.newton_iterations,

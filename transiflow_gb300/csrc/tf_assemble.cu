@@ -340,6 +340,26 @@ __device__ __forceinline__ void add_linear(const Ctx &c, A &at) {
         add(ic<P>{}, ic<2>{}, ic<off1(2, 0)>{}, -gz);
         add(ic<P>{}, ic<2>{}, ic<off1(2, 1)>{}, gz);
     }
+    if constexpr (DIM == 2 && A::template S<0, 1, 1 + 0 * 3 + 9> >= 0) {
+        // - beta * coriolis (Discretization.py:253-255, 1086-1099): the
+        // linear atom holds 0 - beta * c at these slots, no other linear term
+        // (an F atom without these slots belongs to a problem without it)
+        if (c.p.rossby != 0.0) {
+            const double beta = c.p.rossby;
+            const double *aux = c.p.d_aux;
+            const double cv = (Hpy * Dx * Dz / 2) * aux[j];                 // v row, u column
+            const double cu = (Hpx * Dy * Dz / 2) * aux[c.p.ny + j];        // u row, v column
+            const double lv = 0.0 - beta * cv, lu = 0.0 - beta * cu;
+            add(ic<1>{}, ic<0>{}, ic<0 + 3 * 1 + 9>{}, lv);
+            add(ic<1>{}, ic<0>{}, ic<0 + 3 * 2 + 9>{}, lv);
+            add(ic<1>{}, ic<0>{}, ic<1 + 3 * 1 + 9>{}, lv);
+            add(ic<1>{}, ic<0>{}, ic<1 + 3 * 2 + 9>{}, lv);
+            add(ic<0>{}, ic<1>{}, ic<1 + 3 * 0 + 9>{}, lu);
+            add(ic<0>{}, ic<1>{}, ic<2 + 3 * 0 + 9>{}, lu);
+            add(ic<0>{}, ic<1>{}, ic<1 + 3 * 1 + 9>{}, lu);
+            add(ic<0>{}, ic<1>{}, ic<2 + 3 * 1 + 9>{}, lu);
+        }
+    }
     if constexpr (DOF > DIM + 1) {
         constexpr int T = DIM + 1;
         const double cond = c.p.cond;
@@ -528,7 +548,9 @@ __device__ __forceinline__ void boundaries(const Ctx &c, Atom<DIM, DOF, FONLY> &
 // ---------------------------------------------------------------------------
 constexpr double DROP = 1e-14;   // CrsMatrix.compress threshold
 
-template <int DIM, int DOF, bool WF, bool WJ>
+// COR: a 2D problem with the Coriolis term, whose F atom then also holds the
+// velocity-velocity couplings (the full template).
+template <int DIM, int DOF, bool WF, bool WJ, bool COR = false>
 __global__ void __launch_bounds__(128) assemble_kernel(const tf_problem p, const double *__restrict__ st,
                                                        double *__restrict__ rhs, double *__restrict__ jv) {
     const int ncell = p.nx * p.ny * p.nz;
@@ -536,14 +558,14 @@ __global__ void __launch_bounds__(128) assemble_kernel(const tf_problem p, const
     if (cell >= ncell) return;
     Ctx c{p, st, cell % p.nx, (cell / p.nx) % p.ny, cell / (p.nx * p.ny)};
 
-    Atom<DIM, DOF, true> F;
+    Atom<DIM, DOF, !COR> F;
     Atom<DIM, DOF, false> J;
     F.zero();
     if constexpr (WJ) J.zero();
     if (p.nonlinear) nonlinear<DIM, DOF, WJ>(c, F, J);
 
     if constexpr (WJ) {
-        using AF = Atom<DIM, DOF, true>;
+        using AF = Atom<DIM, DOF, !COR>;
         using AJ = Atom<DIM, DOF, false>;
         // atomJ += atomF (Discretization.py:363)
         static_for<DOF>([&](auto D1) {
@@ -570,11 +592,20 @@ __global__ void __launch_bounds__(128) assemble_kernel(const tf_problem p, const
         }
     }
     if constexpr (WF) {
-        using AF = Atom<DIM, DOF, true>;
+        using AF = Atom<DIM, DOF, !COR>;
         add_linear<DIM, DOF>(c, F);
         double frc[DOF];
 #pragma unroll
         for (int d = 0; d < DOF; ++d) frc[d] = 0.0;
+        if constexpr (DIM == 2) {
+            // wind stress of the double gyre (Discretization.py:1101-1118):
+            // u equation, every column but the east wall's
+            if (p.wind != 0.0 && c.i < p.nx - 1) {
+                const double *aux = p.d_aux;
+                const double base = -(1 - p.asym) * aux[2 * p.ny + c.j] - p.asym * aux[3 * p.ny + c.j];
+                frc[0] = base * (p.wind * c.m(0, M_HP, c.i) * c.m(1, M_D, c.j) * c.m(2, M_D, c.k));
+            }
+        }
         boundaries(c, F, frc);
         // assemble_rhs (Discretization.py:439-472): per row, the products in
         // (oz, oy, ox, d2) order, then + frc
@@ -696,6 +727,23 @@ extern "C" int tf_stencil_pattern(const tf_problem *p, int32_t *d_rowptr, int32_
     return cuda_status();
 }
 
+template <int D, int F, bool COR>
+static void launch_assemble_c(int blocks, cudaStream_t s, const tf_problem &p, const double *st, double *rhs,
+                              double *jv) {
+    if (rhs && jv) assemble_kernel<D, F, true, true, COR><<<blocks, 128, 0, s>>>(p, st, rhs, jv);
+    else if (rhs) assemble_kernel<D, F, true, false, COR><<<blocks, 128, 0, s>>>(p, st, rhs, jv);
+    else assemble_kernel<D, F, false, true, COR><<<blocks, 128, 0, s>>>(p, st, rhs, jv);
+}
+
+template <int D, int F>
+static void launch_assemble(bool cor, int blocks, cudaStream_t s, const tf_problem &p, const double *st,
+                            double *rhs, double *jv) {
+    if constexpr (D == 2) {
+        if (cor) { launch_assemble_c<D, F, true>(blocks, s, p, st, rhs, jv); return; }
+    }
+    launch_assemble_c<D, F, false>(blocks, s, p, st, rhs, jv);
+}
+
 extern "C" int tf_assemble(const tf_problem *p, const double *d_state, double *d_rhs, double *d_jvals,
                            tf_stream_t stream) {
     int e = check_problem(p);
@@ -704,11 +752,10 @@ extern "C" int tf_assemble(const tf_problem *p, const double *d_state, double *d
     const int ncell = p->nx * p->ny * p->nz;
     const int blocks = (ncell + 127) / 128;
     cudaStream_t s = (cudaStream_t)stream;
-#define TF_CALL(D, F)                                                                          \
-    if (d_rhs && d_jvals) assemble_kernel<D, F, true, true><<<blocks, 128, 0, s>>>(*p, d_state, d_rhs, d_jvals); \
-    else if (d_rhs) assemble_kernel<D, F, true, false><<<blocks, 128, 0, s>>>(*p, d_state, d_rhs, d_jvals);       \
-    else assemble_kernel<D, F, false, true><<<blocks, 128, 0, s>>>(*p, d_state, d_rhs, d_jvals); \
-    launched()
+    if (p->rossby != 0.0 && p->dim != 2) return TF_ERR_UNSUPPORTED;
+    if ((p->rossby != 0.0 || p->wind != 0.0) && !p->d_aux) return TF_ERR_ARG;
+    const bool cor = p->rossby != 0.0;
+#define TF_CALL(D, F) launch_assemble<D, F>(cor, blocks, s, *p, d_state, d_rhs, d_jvals); launched()
     TF_DISPATCH(p->dim, p->dof, TF_CALL);
 #undef TF_CALL
     return cuda_status();

@@ -16,9 +16,7 @@
 // The reference this replaces is SuperLU via scipy.sparse.linalg.splu
 // (transiflow/interface/SciPy.py:151, 194-202).
 
-#include "tf_common.cuh"
-
-#include <cooperative_groups.h>
+#include "tf_nd.cuh"
 
 #include <algorithm>
 #include <map>
@@ -27,415 +25,6 @@
 
 namespace tf {
 namespace nd {
-
-namespace cg = cooperative_groups;
-
-constexpr int NB = 32;       // panel width
-constexpr int TM = 64;       // gemm tile rows
-constexpr int TN = 64;       // gemm tile cols
-constexpr int THREADS = 256;
-
-struct DevPlan {
-    const int32_t *n_own, *f, *parent, *idx, *ea_map, *rank;
-    const int64_t *front_off, *idx_off, *ea_off, *piv_off;
-};
-
-template <typename T>
-__device__ __forceinline__ T tabs(T x) { return x < T(0) ? -x : x; }
-
-// Pivoted LU of columns [k, k+nb) over own rows [k, n), row swaps applied to
-// the whole front row.  One CTA per front.
-template <typename T>
-__global__ void __launch_bounds__(THREADS) panel_kernel(DevPlan P, int node0, int k, T *fronts, int32_t *piv,
-                                                        int32_t *info) {
-    const int node = node0 + blockIdx.x;
-    const int n = P.n_own[node], f = P.f[node];
-    if (k >= n) return;
-    const int nb = min(NB, n - k);
-    T *F = fronts + P.front_off[node];
-    int32_t *pv = piv + P.piv_off[node];
-    __shared__ T sval[THREADS / 32];
-    __shared__ int sidx[THREADS / 32];
-    __shared__ int s_best;
-    for (int c = k; c < k + nb; ++c) {
-        // pivot search over own rows [c, n)
-        T best = T(-1);
-        int bi = c;
-        for (int r = c + threadIdx.x; r < n; r += THREADS) {
-            T a = tabs(F[(size_t)r * f + c]);
-            if (a > best) { best = a; bi = r; }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            T ob = __shfl_down_sync(0xffffffffu, best, o);
-            int oi = __shfl_down_sync(0xffffffffu, bi, o);
-            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        if ((threadIdx.x & 31) == 0) { sval[threadIdx.x >> 5] = best; sidx[threadIdx.x >> 5] = bi; }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            T b = sval[0];
-            int i = sidx[0];
-            for (int w = 1; w < THREADS / 32; ++w)
-                if (sval[w] > b || (sval[w] == b && sidx[w] < i)) { b = sval[w]; i = sidx[w]; }
-            s_best = i;
-            pv[c] = i;
-            if (b == T(0) && info) atomicAdd(info, 1);
-        }
-        __syncthreads();
-        const int r = s_best;
-        if (r != c)
-            for (int j = threadIdx.x; j < f; j += THREADS) {
-                T t = F[(size_t)c * f + j];
-                F[(size_t)c * f + j] = F[(size_t)r * f + j];
-                F[(size_t)r * f + j] = t;
-            }
-        __syncthreads();
-        T p = F[(size_t)c * f + c];
-        if (p == T(0)) p = T(1e-30);   // singular pivot: flagged through info
-        const T rp = T(1) / p;
-        // scale and update the remaining panel columns over own rows below c
-        for (int rr = c + 1 + threadIdx.x; rr < n; rr += THREADS) {
-            T *row = F + (size_t)rr * f;
-            const T l = row[c] * rp;
-            row[c] = l;
-            for (int j = c + 1; j < k + nb; ++j) row[j] -= l * F[(size_t)c * f + j];
-        }
-        __syncthreads();
-    }
-}
-
-// Same panel factorisation with the (n - k) x nb panel staged in shared
-// memory and its rows split over a cluster of CL CTAs (CL SMs: GB300 issues
-// only two FP64 FMAs per SM and cycle, so one SM per panel is slow for the
-// large fronts near the root).  Per column, with one cluster barrier: every
-// CTA pushes its best row (value, index and the row itself) into every CTA's
-// shared memory, and the owner of the diagonal row pushes that row too; after
-// the barrier each CTA picks the same pivot from its local copies (largest
-// magnitude, lowest row on ties), the two owners swap, and every CTA
-// eliminates its own rows.  The exchange buffers alternate between columns.
-// Afterwards each CTA writes its rows back and applies the recorded swaps, in
-// order, to its share of the columns outside the panel.
-constexpr int PSTRIDE = NB + 1;
-
-template <typename T, int CL>
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(THREADS)
-    panel_cluster_kernel(DevPlan P, int node0, int k, T *fronts, int32_t *piv, int32_t *info) {
-    extern __shared__ unsigned char smem_raw[];
-    T *A = reinterpret_cast<T *>(smem_raw);     // [R][PSTRIDE]: panel rows [lo, hi)
-    cg::cluster_group cluster = cg::this_cluster();
-    const int q = (int)cluster.block_rank();
-    const int node = node0 + blockIdx.x / CL;
-    const int n = P.n_own[node], f = P.f[node];
-    if (k >= n) return;    // the same for every CTA of the cluster
-    const int nb = min(NB, n - k);
-    const int rows = n - k;
-    const int R = (rows + CL - 1) / CL;
-    const int lo = min(rows, q * R), hi = min(rows, lo + R);
-    T *F = fronts + P.front_off[node];
-    int32_t *pv = piv + P.piv_off[node];
-    __shared__ T sval[THREADS / 32];
-    __shared__ int sidx[THREADS / 32];
-    __shared__ T cval[2][CL];
-    __shared__ int cidx[2][CL];
-    __shared__ T crow[2][CL][NB];
-    __shared__ T lrow[2][NB];
-    __shared__ int s_piv[NB];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int t = threadIdx.x; t < (hi - lo) * NB; t += THREADS) {
-        const int r = t / NB, c = t % NB;
-        A[r * PSTRIDE + c] = c < nb ? F[(size_t)(k + lo + r) * f + k + c] : T(0);
-    }
-    __syncthreads();
-    for (int lc = 0; lc < nb; ++lc) {
-        const int par = lc & 1;
-        T best = T(-1);
-        int bi = 0x7fffffff;
-        for (int r = max(lo, lc) + threadIdx.x; r < hi; r += THREADS) {
-            const T a = tabs(A[(r - lo) * PSTRIDE + lc]);
-            if (a > best) { best = a; bi = r; }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const T ob = __shfl_down_sync(0xffffffffu, best, o);
-            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        if (lane == 0) { sval[warp] = best; sidx[warp] = bi; }
-        __syncthreads();
-        const int ql = lc / R;
-        if (warp == 0) {
-            T b = sval[0];
-            int i = sidx[0];
-            for (int w = 1; w < THREADS / 32; ++w)
-                if (sval[w] > b || (sval[w] == b && sidx[w] < i)) { b = sval[w]; i = sidx[w]; }
-            const T v = (i < hi && lane < NB) ? A[(i - lo) * PSTRIDE + lane] : T(0);
-            for (int d = 0; d < CL; ++d) {
-                cluster.map_shared_rank(&crow[par][q][0], d)[lane] = v;
-                if (lane == 0) {
-                    *cluster.map_shared_rank(&cval[par][q], d) = b;
-                    *cluster.map_shared_rank(&cidx[par][q], d) = i;
-                }
-            }
-        } else if (warp == 1 && q == ql) {
-            const T v = A[(lc - lo) * PSTRIDE + lane];
-            for (int d = 0; d < CL; ++d) cluster.map_shared_rank(&lrow[par][0], d)[lane] = v;
-        }
-        cluster.sync();
-        T b = T(-1);
-        int r = 0x7fffffff, w = 0;
-        for (int c = 0; c < CL; ++c)
-            if (cval[par][c] > b || (cval[par][c] == b && cidx[par][c] < r)) { b = cval[par][c]; r = cidx[par][c]; w = c; }
-        const T *prow = crow[par][w];
-        if (r >= rows) { r = lc; b = T(0); prow = lrow[par]; }   // no comparable candidate (NaN column)
-        if (threadIdx.x == 0) {
-            s_piv[lc] = r;
-            if (q == 0) {
-                pv[k + lc] = k + r;
-                if (b == T(0) && info) atomicAdd(info, 1);
-            }
-        }
-        if (r != lc && threadIdx.x < NB) {
-            if (q == ql) A[(lc - lo) * PSTRIDE + threadIdx.x] = prow[threadIdx.x];
-            if (r >= lo && r < hi) A[(r - lo) * PSTRIDE + threadIdx.x] = lrow[par][threadIdx.x];
-        }
-        __syncthreads();
-        T p = prow[lc];
-        if (p == T(0)) p = T(1e-30);   // singular pivot: flagged through info
-        const T rp = T(1) / p;
-        for (int rr = max(lo, lc + 1) + threadIdx.x; rr < hi; rr += THREADS) {
-            T *row = A + (rr - lo) * PSTRIDE;
-            const T l = row[lc] * rp;
-            row[lc] = l;
-            for (int j = lc + 1; j < nb; ++j) row[j] -= l * prow[j];
-        }
-        __syncthreads();
-    }
-    for (int t = threadIdx.x; t < (hi - lo) * NB; t += THREADS) {
-        const int r = t / NB, c = t % NB;
-        if (c < nb) F[(size_t)(k + lo + r) * f + k + c] = A[r * PSTRIDE + c];
-    }
-    // the swaps, in order, on this CTA's share of the columns outside the panel
-    const int other = f - nb, C = (other + CL - 1) / CL;
-    const int c0 = min(other, q * C), c1 = min(other, c0 + C);
-    for (int j = c0 + threadIdx.x; j < c1; j += THREADS) {
-        const int col = j < k ? j : j + nb;
-        for (int lc = 0; lc < nb; ++lc) {
-            const int r = s_piv[lc];
-            if (r != lc) {
-                T *ra = F + (size_t)(k + lc) * f + col;
-                T *rb = F + (size_t)(k + r) * f + col;
-                const T t = *ra;
-                *ra = *rb;
-                *rb = t;
-            }
-        }
-    }
-}
-
-// Row swaps of a finished panel applied to this CTA's share [c0, c1) of the
-// columns outside the panel (column j maps to j < k ? j : j + nb).  The
-// swap sequence (row lc <-> row piv[lc], in order) only moves rows among
-// S = [0, nb) and the distinct pivot rows >= nb, at most 2 nb rows; the
-// composed permutation is worked out once, then the touched rows are
-// gathered through shared memory 64 columns at a time, one round trip per
-// chunk instead of nb dependent ones per column.  stage holds 2 NB x 64
-// values; s_piv holds the pivot rows relative to k.
-constexpr int SWAP_CHUNK = 64;
-
-template <typename T>
-__device__ void apply_panel_swaps(T *F, int f, int k, int nb, int c0, int c1, const int *s_piv, T *stage,
-                                  int nthreads) {
-    __shared__ int sl[2 * NB];     // touched rows (relative to k)
-    __shared__ int pc[NB];         // compact slot of s_piv[t]
-    __shared__ int srcc[2 * NB];   // slot whose old content ends in slot c
-    __shared__ int nsl;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (warp == 0) {
-        const int p = lane < nb ? s_piv[lane] : -1;
-        int first = lane;
-        for (int t = 0; t < lane; ++t)
-            if (s_piv[t] == p) { first = t; break; }
-        const bool extra = p >= nb && first == lane;
-        const unsigned ball = __ballot_sync(0xffffffffu, extra);
-        if (lane < nb) sl[lane] = lane;
-        if (extra) sl[nb + __popc(ball & ((1u << lane) - 1u))] = p;
-        if (lane < nb) pc[lane] = p < nb ? p : nb + __popc(ball & ((1u << first) - 1u));
-        if (lane == 0) nsl = nb + __popc(ball);
-        __syncwarp();
-        if (lane == 0) {
-            int cur[2 * NB];
-            const int m = nsl;
-            for (int c = 0; c < m; ++c) cur[c] = c;
-            for (int t = 0; t < nb; ++t) {
-                const int a = t, b = pc[t];
-                const int x = cur[a];
-                cur[a] = cur[b];
-                cur[b] = x;
-            }
-            for (int c = 0; c < m; ++c) srcc[c] = cur[c];
-        }
-    }
-    __syncthreads();
-    const int m = nsl;
-    for (int j0 = c0; j0 < c1; j0 += SWAP_CHUNK) {
-        const int w = min(SWAP_CHUNK, c1 - j0);
-        for (int t = threadIdx.x; t < m * SWAP_CHUNK; t += nthreads) {
-            const int c = t / SWAP_CHUNK, j = t % SWAP_CHUNK;
-            if (j < w) {
-                const int col = j0 + j < k ? j0 + j : j0 + j + nb;
-                stage[c * SWAP_CHUNK + j] = F[(size_t)(k + sl[c]) * f + col];
-            }
-        }
-        __syncthreads();
-        for (int t = threadIdx.x; t < m * SWAP_CHUNK; t += nthreads) {
-            const int c = t / SWAP_CHUNK, j = t % SWAP_CHUNK;
-            if (j < w && srcc[c] != c) {
-                const int col = j0 + j < k ? j0 + j : j0 + j + nb;
-                F[(size_t)(k + sl[c]) * f + col] = stage[srcc[c] * SWAP_CHUNK + j];
-            }
-        }
-        __syncthreads();
-    }
-}
-
-// Panel factorisation with every panel row held in the registers of one
-// thread (PT threads, one row each, rows split over a cluster of CL CTAs).
-// Per column: a warp all-reduce finds each warp's best row, whose lane parks
-// the row in shared memory; warp 0 picks the CTA's best and pushes value,
-// index and row into every CTA of the cluster (the holder of the diagonal
-// row pushes that row too); after the one cluster barrier every thread picks
-// the same pivot from its local copies, and the swap and the elimination
-// happen in registers.  The exchange buffers alternate between columns,
-// which makes the cluster barrier the only barrier per column.
-template <typename T, int CL, int PT>
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
-    panel_reg_kernel(DevPlan P, int node0, int k, T *fronts, int32_t *piv, int32_t *info) {
-    extern __shared__ unsigned char smem_raw[];
-    T *stage = reinterpret_cast<T *>(smem_raw);   // [2 NB][SWAP_CHUNK] for the swaps
-    constexpr int NW = PT / 32;
-    cg::cluster_group cluster = cg::this_cluster();
-    const int q = (int)cluster.block_rank();
-    const int node = node0 + blockIdx.x / CL;
-    const int n = P.n_own[node], f = P.f[node];
-    if (k >= n) return;    // the same for every CTA of the cluster
-    const int nb = min(NB, n - k);
-    const int rows = n - k;
-    const int R = (rows + CL - 1) / CL;   // <= PT (host-checked)
-    const int lo = min(rows, q * R), hi = min(rows, lo + R);
-    T *F = fronts + P.front_off[node];
-    int32_t *pv = piv + P.piv_off[node];
-    __shared__ T wrow[NW][NB];
-    __shared__ T wval[NW];
-    __shared__ int widx[NW];
-    __shared__ T lstage[NB];
-    __shared__ T cval[2][CL];
-    __shared__ T crcp[2][CL];      // 1 / (candidate's entry in column lc)
-    __shared__ int cidx[2][CL];
-    __shared__ T crow[2][CL][NB];
-    __shared__ T lrow[2][NB];
-    __shared__ int s_piv[NB];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int my = lo + threadIdx.x;
-    const bool have = my < hi;
-    T a[NB];
-    {
-        const T *src = F + (size_t)(k + (have ? my : 0)) * f + k;
-#pragma unroll
-        for (int c = 0; c < NB; ++c) a[c] = (have && c < nb) ? src[c] : T(0);
-    }
-#pragma unroll
-    for (int lc = 0; lc < NB; ++lc) {
-        if (lc < nb) {
-            const int par = lc & 1;
-            const int ql = lc / R;
-            T best = (have && my >= lc) ? tabs(a[lc]) : T(-1);
-            int bi = (have && my >= lc) ? my : 0x7fffffff;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const T ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-            }
-            if (have && bi == my) {
-#pragma unroll
-                for (int c = 0; c < NB; ++c) wrow[warp][c] = a[c];
-            }
-            if (lane == 0) { wval[warp] = best; widx[warp] = bi; }
-            if (have && my == lc) {
-#pragma unroll
-                for (int c = 0; c < NB; ++c) lstage[c] = a[c];
-            }
-            __syncthreads();
-            if (warp == 0) {
-                T b = wval[0];
-                int i = widx[0], ws = 0;
-                for (int w = 1; w < NW; ++w)
-                    if (wval[w] > b || (wval[w] == b && widx[w] < i)) { b = wval[w]; i = widx[w]; ws = w; }
-                const T v = i < rows ? wrow[ws][lane] : T(0);
-                T rcp = T(0);
-                if (lane == lc) rcp = T(1) / (v == T(0) ? T(1e-30) : v);   // singular pivot: flagged through info
-                for (int d = 0; d < CL; ++d) {
-                    cluster.map_shared_rank(&crow[par][q][0], d)[lane] = v;
-                    if (lane == 0) {
-                        *cluster.map_shared_rank(&cval[par][q], d) = b;
-                        *cluster.map_shared_rank(&cidx[par][q], d) = i;
-                    }
-                    if (lane == lc) *cluster.map_shared_rank(&crcp[par][q], d) = rcp;
-                }
-            } else if (warp == 1 && q == ql) {
-                const T v = lstage[lane];
-                for (int d = 0; d < CL; ++d) cluster.map_shared_rank(&lrow[par][0], d)[lane] = v;
-            }
-            cluster.sync();
-            T b = T(-1);
-            int r = 0x7fffffff, w = 0;
-#pragma unroll
-            for (int c = 0; c < CL; ++c)
-                if (cval[par][c] > b || (cval[par][c] == b && cidx[par][c] < r)) { b = cval[par][c]; r = cidx[par][c]; w = c; }
-            const T *prow = crow[par][w];
-            T rp = crcp[par][w];
-            if (r >= rows) {   // no comparable candidate (NaN column)
-                r = lc;
-                b = T(0);
-                prow = lrow[par];
-                rp = T(1) / prow[lc];
-            }
-            if (threadIdx.x == 0) {
-                s_piv[lc] = r;
-                if (q == 0) {
-                    pv[k + lc] = k + r;
-                    if (b == T(0) && info) atomicAdd(info, 1);
-                }
-            }
-            if (have) {
-                if (my == lc) {
-#pragma unroll
-                    for (int c = 0; c < NB; ++c) a[c] = prow[c];
-                } else {
-                    if (my == r) {
-#pragma unroll
-                        for (int c = 0; c < NB; ++c) a[c] = lrow[par][c];
-                    }
-                    if (my > lc) {
-                        const T l = a[lc] * rp;
-                        a[lc] = l;
-#pragma unroll
-                        for (int j = lc + 1; j < NB; ++j) a[j] -= l * prow[j];
-                    }
-                }
-            }
-        }
-    }
-    if (have) {
-        T *dst = F + (size_t)(k + my) * f + k;
-#pragma unroll
-        for (int c = 0; c < NB; ++c)
-            if (c < nb) dst[c] = a[c];
-    }
-    __syncthreads();
-    const int other = f - nb, C = (other + CL - 1) / CL;
-    const int c0 = min(other, q * C), c1 = min(other, c0 + C);
-    apply_panel_swaps(F, f, k, nb, c0, c1, s_piv, stage, PT);
-}
 
 // The two triangular solves with the panel's diagonal block run one row (or
 // column) per thread in small CTAs, so that even a single large front spreads
@@ -856,7 +445,7 @@ static int check_plan(const tf_nd_plan *p) {
 // static shared memory) needs a per-kernel opt-in on the current device.
 // Returns TF_ERR_SIZE when static plus dynamic shared memory would exceed
 // what one CTA can have.
-static int ensure_smem(const void *kernel, size_t bytes) {
+int ensure_smem(const void *kernel, size_t bytes) {
     static std::mutex mu;
     static std::map<std::pair<const void *, int>, size_t> allowed;
     int dev = 0;
@@ -882,79 +471,6 @@ static int ensure_smem(const void *kernel, size_t bytes) {
         return TF_ERR_CUDA;
     }
     allowed[key] = bytes;
-    return TF_OK;
-}
-
-// Panel launch over a cluster of CL CTAs per front.  Returns TF_ERR_SIZE when
-// the per-CTA share of the panel does not fit in shared memory.
-template <typename T, int CL>
-static int launch_panel(const DevPlan &D, int node0, int cnt, int k, int rows, T *fronts, int32_t *piv,
-                        int32_t *info, cudaStream_t s) {
-    const size_t sm = sizeof(T) * (size_t)((rows + CL - 1) / CL) * PSTRIDE;
-    const int e = ensure_smem((const void *)panel_cluster_kernel<T, CL>, sm);
-    if (e) return e;
-    panel_cluster_kernel<T, CL><<<cnt * CL, THREADS, sm, s>>>(D, node0, k, fronts, piv, info);
-    launched();
-    return TF_OK;
-}
-
-// Cluster size for cnt fronts with up to `rows` panel rows: about one CTA per
-// SM in total and at least 32 rows per CTA.
-static int panel_cluster_size(int cnt, int rows, int nsm) {
-    int cl = 8;
-    while (cl > 1 && (cnt * cl > nsm || rows < 32 * cl)) cl >>= 1;
-    return cl;
-}
-
-template <typename T, int CL, int PT>
-static int launch_panel_reg(const DevPlan &D, int node0, int cnt, int k, T *fronts, int32_t *piv, int32_t *info,
-                            cudaStream_t s) {
-    const size_t sm = sizeof(T) * 2 * NB * SWAP_CHUNK;
-    const int e = ensure_smem((const void *)panel_reg_kernel<T, CL, PT>, sm);
-    if (e) return e;
-    panel_reg_kernel<T, CL, PT><<<cnt * CL, PT, sm, s>>>(D, node0, k, fronts, piv, info);
-    launched();
-    return TF_OK;
-}
-
-template <typename T, int CL>
-static int launch_panel_reg_pt(const DevPlan &D, int node0, int cnt, int k, int rows, T *fronts, int32_t *piv,
-                               int32_t *info, cudaStream_t s) {
-    const int R = (rows + CL - 1) / CL;
-    if (R <= 128) return launch_panel_reg<T, CL, 128>(D, node0, cnt, k, fronts, piv, info, s);
-    if (R <= 256) return launch_panel_reg<T, CL, 256>(D, node0, cnt, k, fronts, piv, info, s);
-    if (R <= 512) return launch_panel_reg<T, CL, 512>(D, node0, cnt, k, fronts, piv, info, s);
-    return TF_ERR_SIZE;
-}
-
-template <typename T>
-static int panel(const DevPlan &D, int node0, int cnt, int k, int rows, int nsm, T *fronts, int32_t *piv,
-                 int32_t *info, cudaStream_t s) {
-    // one register-held row per thread while a cluster of up to 8 CTAs
-    // offers at most 512 rows per CTA
-    for (int cl = panel_cluster_size(cnt, rows, nsm); cl <= 8; cl *= 2) {
-        int e = TF_ERR_SIZE;
-        switch (cl) {
-        case 1: e = launch_panel_reg_pt<T, 1>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
-        case 2: e = launch_panel_reg_pt<T, 2>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
-        case 4: e = launch_panel_reg_pt<T, 4>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
-        default: e = launch_panel_reg_pt<T, 8>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
-        }
-        if (e != TF_ERR_SIZE) return e;
-    }
-    // larger panels: rows staged in shared memory
-    for (int cl = panel_cluster_size(cnt, rows, nsm); cl <= 8; cl *= 2) {
-        int e = TF_ERR_SIZE;
-        switch (cl) {
-        case 1: e = launch_panel<T, 1>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
-        case 2: e = launch_panel<T, 2>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
-        case 4: e = launch_panel<T, 4>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
-        default: e = launch_panel<T, 8>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
-        }
-        if (e != TF_ERR_SIZE) return e;
-    }
-    panel_kernel<T><<<cnt, THREADS, 0, s>>>(D, node0, k, fronts, piv, info);
-    launched();
     return TF_OK;
 }
 

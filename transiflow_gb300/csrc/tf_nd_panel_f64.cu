@@ -1,0 +1,11 @@
+// The panel factorisations in FP64 (see tf_nd_panel.cuh).
+
+#include "tf_nd_panel.cuh"
+
+namespace tf {
+namespace nd {
+
+template int panel<double>(const DevPlan &, int, int, int, int, int, double *, int32_t *, int32_t *, cudaStream_t);
+
+}  // namespace nd
+}  // namespace tf

@@ -193,7 +193,8 @@ class BoundaryProgram:
 
 def builtin_boundaries(parameters, bc, dim, nz):
     """The call sequences of Discretization._lid_driven_cavity,
-    _rayleigh_benard and _differentially_heated_cavity (Discretization.py:577-643)."""
+    _rayleigh_benard, _differentially_heated_cavity and _double_gyre
+    (Discretization.py:577-655)."""
     problem = parameters.get('Problem Type', 'Lid-driven Cavity').lower()
     if problem == 'lid-driven cavity':
         v = get_parameter(parameters, 'Lid Velocity', 1)
@@ -228,6 +229,13 @@ def builtin_boundaries(parameters, bc, dim, nz):
         bc.temperature_bottom(None, bottom)
         bc.free_slip_top()
         bc.no_slip_bottom()
+    elif problem == 'double gyre':
+        # Discretization._double_gyre (Discretization.py:645-655); the wind
+        # stress itself is a forcing of the kernel (tf_problem.wind)
+        bc.no_slip_east()
+        bc.no_slip_west()
+        bc.free_slip_north()
+        bc.free_slip_south()
     elif problem == 'differentially heated cavity':
         bc.temperature_east(None, -1 / 2)
         bc.temperature_west(None, 1 / 2)
@@ -252,8 +260,9 @@ def scalars(parameters, dim, dof, nz):
     Ra = get_parameter(parameters, 'Rayleigh Number', 1.0)
     Pr = get_parameter(parameters, 'Prandtl Number', 1.0)
     Gr = get_parameter(parameters, 'Grashof Number', Ra / Pr)
-    if get_parameter(parameters, 'Rossby Parameter'):
-        raise NotImplementedError('the Coriolis term is not available on the GPU backend')
+    rossby = get_parameter(parameters, 'Rossby Parameter')
+    if rossby and dim != 2:
+        raise NotImplementedError('the Coriolis term exists in 2D only (Discretization.py:253-255)')
     if dof > dim + 2:
         raise NotImplementedError('salinity is not available on the GPU backend')
     if Re == 0:
@@ -272,12 +281,29 @@ def scalars(parameters, dim, dof, nz):
         Bi = get_parameter(parameters, 'Biot Number')
         biot_row = 2 if (dim == 3 and nz > 1) else 1
         biot = Bi / (Bi + 1)
+    wind = 0.0
+    if problem == 'double gyre':
+        wind = get_parameter(parameters, 'Wind Stress Parameter') / (2 * np.pi)
     return dict(visc=float(visc), cond=float(cond), nonlinear=int(nonlinear),
-                buoy_row=buoy_row, biot_row=biot_row, biot=float(biot))
+                buoy_row=buoy_row, biot_row=biot_row, biot=float(biot), rossby=float(rossby),
+                wind=float(wind), asym=float(get_parameter(parameters, 'Asymmetry Parameter')))
 
 
-def make_problem(parameters, nx, ny, nz, dim, dof, x, y, z, d_metric, stride, boundary_conditions=None):
-    """Fill the tf_problem structure for the current parameter values."""
+def aux_table(y, ny):
+    """Per-row factors of the Coriolis term and the wind stress
+    (Discretization.py:1086-1118), computed with the reference's operations:
+    y[j]/2, -(y[j]+y[j-1])/4, cos(2 pi yc), cos(pi yc) for yc = (y[j]+y[j-1])/2."""
+    j = np.arange(ny)
+    yj, yjm = y[j], y[j - 1]
+    yc = (yj + yjm) / 2
+    return np.stack([yj / 2, -(yj + yjm) / 4, np.cos(2 * np.pi * yc), np.cos(np.pi * yc)])
+
+
+def make_problem(parameters, nx, ny, nz, dim, dof, x, y, z, d_metric, stride, boundary_conditions=None,
+                 d_aux=None):
+    """Fill the tf_problem structure for the current parameter values
+    (d_aux: device copy of aux_table(y, ny), needed for the Coriolis term and
+    the wind stress)."""
     sc = scalars(parameters, dim, dof, nz)
     bc = BoundaryProgram(nx, ny, nz, dim, dof, x, y, z)
     if boundary_conditions is None:
@@ -297,4 +323,8 @@ def make_problem(parameters, nx, ny, nz, dim, dof, x, y, z, d_metric, stride, bo
     p.nops = len(bc.ops)
     for t, (kind, axis, high, var, fc, ac) in enumerate(bc.ops):
         p.ops[t] = _lib.BcOp(kind, axis, high, var, fc, ac)
+    p.rossby, p.wind, p.asym = sc['rossby'], sc['wind'], sc['asym']
+    if (p.rossby or p.wind) and not d_aux:
+        raise ValueError('the Coriolis term and the wind stress need the aux table')
+    p.d_aux = d_aux
     return p

@@ -89,6 +89,7 @@ class Interface:
         table = grid.metric_table((self.x, self.y, self.z), (nx, ny, nz))
         self._metric = torch.as_tensor(table.ravel()).to(self.device)
         self._stride = table.shape[2]
+        self._aux = torch.as_tensor(grid.aux_table(self.y, ny).ravel()).to(self.device)
         # validate the problem type and boundary program now
         self._problem()
         # pattern of the stencil CSR
@@ -135,7 +136,7 @@ class Interface:
     def _problem(self):
         return grid.make_problem(self.parameters, self.nx, self.ny, self.nz, self.dim, self.dof,
                                  self.x, self.y, self.z, self._metric.data_ptr(), self._stride,
-                                 self.boundary_conditions)
+                                 self.boundary_conditions, self._aux.data_ptr())
 
     # -- vectors -----------------------------------------------------------------
     def vector(self):

@@ -30,6 +30,7 @@ from .vector import DeviceVector, _stream
 # interfaces of the same shape share one (keyed by shape and device).
 _PLANS = {}
 _PLANS_LOCK = threading.Lock()
+_CAPTURE_LOCK = threading.Lock()
 
 
 class NdPlanDevice:
@@ -146,21 +147,29 @@ class _Graphed:
             self.fn()
             return
         lib = _lib.load()
-        torch.cuda.synchronize()
-        g = torch.cuda.CUDAGraph()
-        before = lib.tf_launch_count()
-        # capture on this thread's stream unless it is the default stream
-        # (torch's shared side stream is then used), so that threads driving
-        # instances on their own streams can capture concurrently
+        # Captured with capture_begin/capture_end on a non-default stream of
+        # this thread (torch.cuda.graph would synchronise the whole device,
+        # which fails while another thread's stream is capturing), one
+        # capture at a time.
         cur = torch.cuda.current_stream()
-        kw = {} if cur == torch.cuda.default_stream() else {'stream': cur}
-        try:
-            with torch.cuda.graph(g, capture_error_mode='thread_local', **kw):
+        side = cur if cur != torch.cuda.default_stream() else torch.cuda.Stream()
+        g = torch.cuda.CUDAGraph()
+        with _CAPTURE_LOCK:
+            side.wait_stream(cur)
+            before = lib.tf_launch_count()
+            try:
+                with torch.cuda.stream(side):
+                    g.capture_begin(capture_error_mode='thread_local')
+                    try:
+                        self.fn()
+                    finally:
+                        g.capture_end()
+            except RuntimeError:
+                self.failed = True
+                cur.wait_stream(side)
                 self.fn()
-        except RuntimeError:
-            self.failed = True
-            self.fn()
-            return
+                return
+            cur.wait_stream(side)
         self.kernels = lib.tf_launch_count() - before
         self.graph = g
         g.replay()
@@ -248,6 +257,11 @@ class Solver:
         # adapted: halved after a failed attempt, grown after a success
         self._drift_tol = reuse_drift
         self._drift_work = None
+        # solves per operator and GMRES iterations with a fresh factorisation
+        self._solves_per_op = 1.0
+        self._its_fresh = 1.0
+        self._last_op = None
+        self._last_op_solves = 0
         self.gauge = interface.pressure_row if interface.dof > interface.dim else -1
         self.restart = restart
         self.tol = tol
@@ -272,6 +286,9 @@ class Solver:
                 plan = _PLANS.get(key)
                 if plan is None:
                     plan = NdPlanDevice(pattern, itf.nx, itf.ny, itf.nz, itf.dof, pvar)
+                    # the uploads ran on this thread's stream: finish them
+                    # before another thread's stream can read the plan
+                    torch.cuda.current_stream().synchronize()
                     _PLANS[key] = plan
             self.plan = plan
             self.info = torch.zeros(1, dtype=torch.int32, device=pattern.rowptr.device)
@@ -472,26 +489,49 @@ class Solver:
             return self.reuse_maxit
         if self._cost_factor is None or self._cost_iter is None:
             return self.reuse_maxit
-        return int(min(self.reuse_maxit, self._cost_factor / self._cost_iter))
+        # a Jacobian serves about m solves (two per continuation corrector
+        # step); reusing costs m times the iterations, refactoring costs one
+        # factorisation plus m times the iterations of a fresh factorisation
+        m = self._solves_per_op
+        its_f = self._its_fresh
+        return int(min(self.reuse_maxit, (self._cost_factor / self._cost_iter + m * its_f) / m))
+
+    def _count_solve(self, op):
+        if op is not self._last_op:
+            if self._last_op is not None:
+                self._solves_per_op = 0.8 * self._solves_per_op + 0.2 * self._last_op_solves
+            self._last_op, self._last_op_solves = op, 0
+        self._last_op_solves += 1
 
     def _solve_gauged(self, op, b):
         """x with A_g x = b to the tolerance, reusing the latest factorisation
         as preconditioner while that is cheaper than refactoring."""
+        self._count_solve(op)
         own = op.jac.lu
         if isinstance(own, Factorization) and own.valid() and own.precision == self.precision:
-            return self.fgmres(op, own, b)
+            x, its, rr = self.fgmres(op, own, b)
+            self._its_fresh = 0.8 * self._its_fresh + 0.2 * its
+            return x, its, rr
         prec = self._prec
         limit = self._reuse_limit() if self.reuse else 0
+        seen = getattr(op, '_reuse_its', None)
+        if seen is not None and self.reuse_policy != 'always' and self._cost_factor and self._cost_iter:
+            # a reuse on this operator already took `seen` iterations: refactor
+            # now if that is dearer than a factorisation
+            limit = 0 if seen * self._cost_iter > self._cost_factor + self._its_fresh * self._cost_iter else limit
         if limit >= 2 and prec is not None and prec.valid() and prec.precision == self.precision:
-            if self.reuse_policy == 'always' or self._drift(op) <= self._drift_tol:
+            if self.reuse_policy == 'always' or seen is not None or self._drift(op) <= self._drift_tol:
                 x, its, rr = self.fgmres(op, prec, b, maxit=limit)
                 if math.isfinite(rr) and rr <= self.tol:
                     self.stats['reused'] += 1
+                    op._reuse_its = its
                     self._drift_tol = min(0.5, 1.25 * self._drift_tol)
                     return x, its, rr
                 self.stats['refactored_after_reuse'] += 1
                 self._drift_tol *= 0.5
-        return self.fgmres(op, self.factorize(op), b)
+        x, its, rr = self.fgmres(op, self.factorize(op), b)
+        self._its_fresh = 0.8 * self._its_fresh + 0.2 * its
+        return x, its, rr
 
     def _drift(self, op):
         """||A_new - A_f|| / ||A_f|| over the stencil values, A_f being the

@@ -178,7 +178,9 @@ _work = {}
 def _dot(a, b):
     lib = _lib.load()
     n = a.size
-    key = a.data.device
+    # one workspace per stream: threads driving instances on their own
+    # streams must not share partial sums
+    key = (a.data.device, torch.cuda.current_stream().cuda_stream)
     need = lib.tf_vec_mdot_workspace_bytes(n, 1)
     buf = _work.get(key)
     if buf is None or buf.numel() * 8 < need + 8:
