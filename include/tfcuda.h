@@ -55,7 +55,7 @@ enum {
 
 #define TF_MAX_BC_OPS 24
 
-enum { TF_BC_WALL = 1, TF_BC_FORCE = 2 };
+enum { TF_BC_WALL = 1, TF_BC_FORCE = 2, TF_BC_FORCE_PROFILE = 3, TF_BC_PIN = 4 };
 
 /* One boundary-condition primitive applied to the atoms of the cells on one
  * face of the box (BoundaryConditions.py:55-544):
@@ -63,8 +63,17 @@ enum { TF_BC_WALL = 1, TF_BC_FORCE = 2 };
  *                BoundaryConditions.py:55-233;
  *   TF_BC_FORCE: _constant_forcing_* with forcing constant fc and atom
  *                constant ac for variable var, BoundaryConditions.py:471-544
- *                (moving lids, fixed temperatures and heat fluxes reduce to
- *                this).                                                       */
+ *                (moving lids, fixed temperatures, heat and salinity fluxes
+ *                reduce to this);
+ *   TF_BC_FORCE_PROFILE: the same with a forcing that varies along the
+ *                face (2D only): the neighbour at tangential index m (m = -1
+ *                is the ghost before the first cell) is forced by
+ *                d_prof[row * prof_len + (m < 0 ? prof_len - 1 : m)] with
+ *                row = (int)fc, as numpy.ones((n + 2, .)) * value indexes it;
+ *   TF_BC_PIN  : fix one value of variable var (Discretization.py:690-702):
+ *                every entry coupling to var of cell (0,0,0), periodic
+ *                neighbours included, becomes 0, that row gets -1 on its
+ *                diagonal and no forcing.  Applied in op order, i.e. last.   */
 typedef struct tf_bc_op {
     int32_t kind;
     int32_t axis;   /* 0 = x, 1 = y, 2 = z                */
@@ -105,6 +114,14 @@ typedef struct tf_problem {
     double wind;
     double asym;
     const double *d_aux;
+    /* salinity (dof = dim + 3): sal = 1 / (Le * Pr * sqrt(Gr))
+     * (Discretization.py:260-263); d_prof / prof_len: the forcing profiles of
+     * TF_BC_FORCE_PROFILE ops, nprof profiles of prof_len values (NULL / 0 if
+     * none). */
+    double sal;
+    const double *d_prof;
+    int32_t prof_len;
+    int32_t nprof;         /* number of profiles in d_prof                   */
 } tf_problem;
 
 /* ---- library ------------------------------------------------------------*/

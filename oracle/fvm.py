@@ -223,15 +223,26 @@ def apply_wall(atom, frc, axis, high, sign):
 
 
 def apply_forcing(atom, frc, axis, high, var, fc, ac):
-    """_constant_forcing_*, BoundaryConditions.py:471-544 (scalar value)."""
+    """_constant_forcing_*, BoundaryConditions.py:471-544.  fc is a scalar or,
+    as ``numpy.ones((n1 + 2, n2 + 2)) * value`` there, an array over the
+    boundary's two other axes including their ghosts, read at
+    [i + o1 - 1, j + o2 - 1] (index -1 meaning the last)."""
     n = atom.shape[axis]
     b = n - 1 if high else 0
     out = 2 if high else 0
     face = atom[_ix(axis, b, d1=var, d2=var, off=out)]     # cells(2) x offsets(2)
     acc = np.zeros(face.shape[:2])
+    n1, n2 = face.shape[:2]
+    if np.ndim(fc):
+        V = np.ones((n1 + 2, n2 + 2)) * fc
+        i1 = np.arange(n1)[:, None]
+        i2 = np.arange(n2)[None, :]
     for o2 in range(3):          # the later offset axis is the outer loop
         for o1 in range(3):
-            acc += face[:, :, o1, o2] * fc
+            if np.ndim(fc):
+                acc += face[:, :, o1, o2] * V[i1 + o1 - 1, i2 + o2 - 1]
+            else:
+                acc += face[:, :, o1, o2] * fc
     fidx = [slice(None)] * 4
     fidx[axis] = b
     fidx[3] = var
@@ -275,7 +286,7 @@ class Discretization:
                 dof = self.dim + 3
         self.dof = dof
         if self.problem not in ('lid-driven cavity', 'differentially heated cavity',
-                                'rayleigh-benard', 'rayleigh-benard perturbation', 'double gyre'):
+                                'rayleigh-benard', 'rayleigh-benard perturbation', 'double gyre', 'amoc'):
             raise NotImplementedError('problem type %s' % self.problem)
         self.zper = nz == 1
         p = parameters
@@ -356,7 +367,12 @@ class Discretization:
                 fa = Hpy * Dx * Dz / 2
                 atom += self._line(1, T, 1, {1: fa, 2: fa})
             if dof > 4:
-                raise NotImplementedError('salinity')
+                Le = self.get_parameter('Lewis Number', 1.0)
+                Sv = dim + 2
+                atom += 1 / (Le * Pr * np.sqrt(Gr)) * (self._second(Sv, Sv, 0, Hx, Hpx, Dy, Dz)
+                                                       + self._second(Sv, Sv, 1, Hy, Hpy, Dx, Dz))
+                fa = Hpy * Dx * Dz / 2
+                atom -= self._line(1, Sv, 1, {1: fa, 2: fa})
             if self.problem == 'rayleigh-benard perturbation':
                 Bi = self.get_parameter('Biot Number')
                 ba = Hpy * Dx * Dz / 2
@@ -385,7 +401,17 @@ class Discretization:
                 fa = Hpy * Dx * Dz / 2
                 atom += self._line(1, T, 1, {1: fa, 2: fa})
         if dof > 5:
-            raise NotImplementedError('salinity')
+            Le = self.get_parameter('Lewis Number', 1.0)
+            Sv = dim + 2
+            atom += 1 / (Le * Pr * np.sqrt(Gr)) * (self._second(Sv, Sv, 0, Hx, Hpx, Dy, Dz)
+                                                   + self._second(Sv, Sv, 1, Hy, Hpy, Dx, Dz)
+                                                   + self._second(Sv, Sv, 2, Hz, Hpz, Dy, Dx))
+            if self.nz > 1:
+                fa = Hpz * Dy * Dx / 2
+                atom -= self._line(2, Sv, 2, {1: fa, 2: fa})
+            else:
+                fa = Hpy * Dx * Dz / 2
+                atom -= self._line(1, Sv, 1, {1: fa, 2: fa})
         if self.problem == 'rayleigh-benard perturbation':
             Bi = self.get_parameter('Biot Number')
             if self.nz > 1:
@@ -567,7 +593,13 @@ class Discretization:
                 # w_C_z, Discretization.py:1447-1459
                 self._scalar_conv(F, J, T, 2, Dy * Dx, S[1:nx + 1, 1:ny + 1, 0:nz + 1, 2], avg(ST, 2))
         if dof > dim + 2:
-            raise NotImplementedError('salinity')
+            Sv = dim + 2
+            SS = S[..., Sv]
+            # u_S_x, v_S_y, w_S_z: u_C_x etc. for the salinity (Discretization.py:1331-1467)
+            self._scalar_conv(F, J, Sv, 0, Dy * Dz, S[0:nx + 1, 1:ny + 1, 1:nz + 1, 0], avg(SS, 0))
+            self._scalar_conv(F, J, Sv, 1, Dx * Dz, S[1:nx + 1, 0:ny + 1, 1:nz + 1, 1], avg(SS, 1))
+            if dim > 2:
+                self._scalar_conv(F, J, Sv, 2, Dy * Dx, S[1:nx + 1, 1:ny + 1, 0:nz + 1, 2], avg(SS, 2))
         J += F
         return J, F
 
@@ -664,6 +696,33 @@ class Discretization:
             wall(0, False)
             wall(1, True, +1)
             wall(1, False, +1)
+        elif p == 'amoc':
+            # Discretization._amoc, Discretization.py:657-702
+            Sv = dim + 2
+
+            def salinity_flux(axis, high, q):
+                c, n = coord(axis)
+                if high:
+                    force(axis, True, Sv, (c[n] - c[n - 2]) / 2 * q, 1)
+                else:
+                    force(axis, False, Sv, -((c[0] - c[-2]) / 2) * q, 1)
+
+            heat_flux(0, True, 0)
+            heat_flux(0, False, 0)
+            salinity_flux(0, True, 0)
+            salinity_flux(0, False, 0)
+            wall(0, True, +1)
+            wall(0, False, +1)
+            heat_flux(1, False, 0)
+            salinity_flux(1, False, 0)
+            wall(1, False, +1)
+            T_S, Q_S = self.amoc_profiles()
+            theta = self.get_parameter('Temperature Forcing')
+            sigma = self.get_parameter('Freshwater Flux')
+            temperature(1, True, theta * T_S)
+            salinity_flux(1, True, sigma * Q_S)
+            wall(1, True, +1)
+            ops.append(('pin', Sv))
         elif p == 'differentially heated cavity':
             temperature(0, True, -1 / 2)
             temperature(0, False, 1 / 2)
@@ -689,9 +748,48 @@ class Discretization:
         for op in self.bc_program():
             if op[0] == 'wall':
                 apply_wall(atom, frc, op[1], op[2], op[3])
+            elif op[0] == 'pin':
+                self.pin(atom, frc, op[1])
             else:
                 apply_forcing(atom, frc, *op[1:])
         return state_vec(frc)
+
+    def pin(self, atom, frc, var):
+        """Fix one value of ``var`` (Discretization.py:690-702): every entry
+        coupling to ``var`` of cell (0, 0, 0), periodic neighbours included,
+        becomes 0, that row gets -1 on its diagonal and no forcing."""
+        nx, ny, nz = self.nx, self.ny, self.nz
+        i = np.arange(nx)[:, None, None, None, None, None]
+        j = np.arange(ny)[None, :, None, None, None, None]
+        k = np.arange(nz)[None, None, :, None, None, None]
+        o = np.arange(3)
+        x, y, z = o[None, None, None, :, None, None], o[None, None, None, None, :, None], \
+            o[None, None, None, None, None, :]
+        hit = (((i + x - 1) % nx) == 0) & (((j + y - 1) % ny) == 0) & (((k + z - 1) % nz) == 0)
+        hit = np.broadcast_to(hit, (nx, ny, nz, 3, 3, 3))
+        for d in range(self.dof):
+            a = atom[:, :, :, d, var]
+            a[hit] = 0
+        atom[0, 0, 0, var, var, 1, 1, 1] = -1
+        frc[0, 0, 0, var] = 0
+
+    def amoc_profiles(self):
+        """T_S and Q_S of Discretization._amoc (Discretization.py:674-689):
+        surface temperature and salinity-flux profiles over the cell centres,
+        shape (nx + 2, nz + 2), set in column 0."""
+        c = self.x
+        x = np.zeros(len(c) - 1)
+        for m in range(-1, len(c) - 2):
+            x[m] = (c[m] + c[m - 1]) / 2
+        asym = self.get_parameter('Asymmetry Parameter')
+        A = self.parameters.get('X-max', 1.0)
+        T_S = np.zeros((self.nx + 2, self.nz + 2))
+        T_S[:, 0] = 1 / 2 * ((1 - asym) * np.cos(2 * np.pi * (x / A - 1 / 2))
+                             + asym * np.cos(np.pi * x / A) + 1)
+        p = 2
+        Q_S = np.zeros((self.nx + 2, self.nz + 2))
+        Q_S[:, 0] = 3 * np.cos(p * np.pi * (x / A - 1 / 2)) - 6 / (p * np.pi) * np.sin(p * np.pi / 2)
+        return T_S, Q_S
 
     # -- assembly (Discretization.py:367-548) ----------------------------------
 
@@ -745,6 +843,8 @@ class Discretization:
             m[..., 2] = np.broadcast_to(Hpz * Dy * Dx, shape)
         if self.dof > self.dim + 1:
             m[..., self.dim + 1] = np.broadcast_to(Dx * Dy * Dz, shape)
+        if self.dof > self.dim + 2:
+            m[..., self.dim + 2] = np.broadcast_to(Dx * Dy * Dz, shape)
         diag = state_vec(m)
         n = len(diag)
         rows = np.arange(n)

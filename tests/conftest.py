@@ -34,7 +34,8 @@ def golden_csr(g, t):
 
 DISC_FIXTURES = ['ldc2d_16_re1000', 'ldc2d_16_re0', 'ldc2d_12x10_stretched', 'ldc3d_4_ramp',
                  'ldc3d_5x4x3_stretched', 'ldc_semi2d_4', 'dhc2d_8_stretched', 'dhc3d_4_ramp',
-                 'rb3d_4_ramp', 'rb2d_6x5', 'rbp2d_6x5', 'qg2d_4_ramp', 'qg2d_8x6']
+                 'rb3d_4_ramp', 'rb2d_6x5', 'rbp2d_6x5', 'qg2d_4_ramp', 'qg2d_8x6',
+                 'amoc2d_4_ramp', 'amoc2d_8x4']
 
 
 @pytest.fixture(scope='session')

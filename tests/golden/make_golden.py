@@ -54,6 +54,12 @@ CASES = [
     ('qg2d_8x6', {'Reynolds Number': 30, 'Rossby Parameter': 500, 'Wind Stress Parameter': 700,
                   'Asymmetry Parameter': 0.3, 'Problem Type': 'Double Gyre'}, 8, 6, 1, None, None,
      ('normal', 6, 2)),
+    ('amoc2d_4_ramp', {'Reynolds Number': 16, 'Rayleigh Number': 4e4, 'Prandtl Number': 2.25,
+                       'Lewis Number': 1, 'Temperature Forcing': 1, 'Freshwater Flux': 1,
+                       'Problem Type': 'AMOC'}, 4, 4, 1, 2, 5, ('ramp',)),
+    ('amoc2d_8x4', {'Rayleigh Number': 4e4, 'Prandtl Number': 2.25, 'Lewis Number': 1.2,
+                    'Temperature Forcing': 0.7, 'Freshwater Flux': 0.1, 'Asymmetry Parameter': 0.2,
+                    'X-max': 5, 'Problem Type': 'AMOC'}, 8, 4, 1, None, None, ('normal', 7, 2)),
 ]
 
 

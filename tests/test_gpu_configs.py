@@ -168,3 +168,35 @@ def test_double_gyre_wind_branch_matches_oracle():
         xg = _gpu_root(itf, 'Wind Stress Parameter', mu, x)
         xr = _oracle_root(QG, (16, 16), 'Wind Stress Parameter', mu, x)
         assert np.linalg.norm(xg - xr) <= 1e-8 * np.linalg.norm(xr)
+
+
+AMOC = {'Problem Type': 'AMOC', 'Rayleigh Number': 4e4, 'Prandtl Number': 2.25, 'X-max': 5}
+
+
+def test_amoc_branches_match_oracle():
+    """The reference's AMOC continuation (test_continuation.py:430-466):
+    temperature forcing 0 -> 1, then freshwater flux 0 -> 0.2, at 16 x 8;
+    every accepted point is a root of the oracle's equations too."""
+    from transiflow_gb300 import Interface
+    itf = Interface(dict(AMOC), 16, 8)
+    pts = _branch(itf, 'Temperature Forcing', 0.0, 1.0, 0.1)
+    assert abs(pts[-1][0] - 1.0) < 1e-3
+    for mu, x in pts[1::3]:
+        itf.set_parameter('Temperature Forcing', mu)
+        assert itf.rhs(itf.vector_from_array(x)).norm() <= 1e-8
+        xg = _gpu_root(itf, 'Temperature Forcing', mu, x)
+        xr = _oracle_root(AMOC, (16, 8), 'Temperature Forcing', mu, x)
+        assert np.linalg.norm(xg - xr) <= 1e-8 * np.linalg.norm(xr)
+    from transiflow_gb300 import Continuation
+    itf.set_parameter('Temperature Forcing', 1.0)
+    cont = Continuation(itf, newton_tolerance=1e-8, quiet=True)
+    fw = []
+    x, mu = cont.continuation(itf.vector_from_array(pts[-1][1]), 'Freshwater Flux', 0.0, 0.2, 0.01,
+                              callback=lambda i, xx, m: fw.append((m, xx.numpy())))
+    assert abs(mu - 0.2) < 1e-3
+    p = dict(AMOC, **{'Temperature Forcing': 1.0})
+    for m, xf in fw[1::4] + [(mu, x.numpy())]:
+        itf.set_parameter('Freshwater Flux', m)
+        xg = _gpu_root(itf, 'Freshwater Flux', m, xf)
+        xr = _oracle_root(p, (16, 8), 'Freshwater Flux', m, xf)
+        assert np.linalg.norm(xg - xr) <= 1e-8 * np.linalg.norm(xr)

@@ -72,6 +72,8 @@ LAYOUT_CASES = [
             'Wind Stress Parameter': 700}, (7, 6, 1)),
     (2, 4, {'Problem Type': 'Double Gyre', 'Reynolds Number': 16, 'Rossby Parameter': 1000,
             'Wind Stress Parameter': 1000}, (5, 6, 1)),
+    (2, 5, {'Problem Type': 'AMOC', 'Rayleigh Number': 4e4, 'Prandtl Number': 2.25, 'Temperature Forcing': 1,
+            'Freshwater Flux': 0.3, 'X-max': 5}, (7, 5, 1)),
 ]
 
 

@@ -140,6 +140,23 @@ def test_oracle_matches_reference_double_gyre_golden_file():
     assert np.allclose(d.rhs(state), rhs_ref, rtol=1e-6, atol=1e-12)
 
 
+@pytest.mark.skipif(not has_reference(), reason='reference golden files not available')
+def test_oracle_matches_reference_amoc_golden_file():
+    """The reference's own AMOC 4x4x1 golden matrix and right-hand side
+    (test_fvm.py:1217-1255, state i+1)."""
+    params = {'Reynolds Number': 16, 'Rayleigh Number': 4e4, 'Prandtl Number': 2.25, 'Lewis Number': 1,
+              'Temperature Forcing': 1, 'Freshwater Flux': 1, 'Problem Type': 'AMOC'}
+    b_ref, c_ref, v_ref = _read_matrix(os.path.join(REFERENCE, 'tests', 'data', 'amoc_4x4x1.txt'))
+    d = fvm.Discretization(dict(params), 4, 4, 1, 2, 5)
+    state = np.arange(1, 4 * 4 * 5 + 1, dtype=np.float64)
+    A = d.jacobian(state)
+    assert np.array_equal(A.begA[:len(b_ref)], b_ref)
+    assert np.array_equal(A.jcoA[:len(c_ref)], c_ref)
+    assert np.allclose(A.coA[:len(v_ref)], v_ref, rtol=1e-6, atol=0)
+    rhs_ref = np.loadtxt(os.path.join(REFERENCE, 'tests', 'data', 'amoc_rhs_4x4x1.txt'))
+    assert np.allclose(d.rhs(state), rhs_ref, rtol=1e-6, atol=1e-12)
+
+
 def test_oracle_solve_matches_fixture():
     g = load_golden('solve_ldc2d_12')
     itf = OracleInterface({'Reynolds Number': float(g['re'])}, 12, 12)

@@ -27,6 +27,8 @@ TF_MAX_BC_OPS = 24
 TF_METRIC_FIELDS = 10
 TF_BC_WALL = 1
 TF_BC_FORCE = 2
+TF_BC_FORCE_PROFILE = 3
+TF_BC_PIN = 4
 
 
 def _nvcc():
@@ -77,7 +79,8 @@ class Problem(ctypes.Structure):
                 ('d_metric', ctypes.c_void_p), ('metric_stride', ctypes.c_int32),
                 ('nops', ctypes.c_int32), ('ops', BcOp * TF_MAX_BC_OPS),
                 ('rossby', ctypes.c_double), ('wind', ctypes.c_double), ('asym', ctypes.c_double),
-                ('d_aux', ctypes.c_void_p)]
+                ('d_aux', ctypes.c_void_p), ('sal', ctypes.c_double), ('d_prof', ctypes.c_void_p),
+                ('prof_len', ctypes.c_int32), ('nprof', ctypes.c_int32)]
 
 
 class NdPlan(ctypes.Structure):

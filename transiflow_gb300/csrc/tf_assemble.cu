@@ -266,6 +266,17 @@ __device__ __forceinline__ void nonlinear(const Ctx &c, AF &F, AJ &J) {
             scalar_conv<T, 2, WJ>(F, J, Dy * Dx, c.s(i, j, k - 1, 2), c.s(i, j, k, 2),
                                   c.avz(T, i, j, k), c.avz(T, i, j, k + 1));
     }
+    if constexpr (DOF > DIM + 2) {
+        // u_S_x, v_S_y (Discretization.py:1331-1400)
+        constexpr int Sv = DIM + 2;
+        scalar_conv<Sv, 0, WJ>(F, J, Dy * Dz, c.s(i - 1, j, k, 0), c.s(i, j, k, 0),
+                               c.avx(Sv, i, j, k), c.avx(Sv, i + 1, j, k));
+        scalar_conv<Sv, 1, WJ>(F, J, Dx * Dz, c.s(i, j - 1, k, 1), c.s(i, j, k, 1),
+                               c.avy(Sv, i, j, k), c.avy(Sv, i, j + 1, k));
+        if constexpr (DIM > 2)
+            scalar_conv<Sv, 2, WJ>(F, J, Dy * Dx, c.s(i, j, k - 1, 2), c.s(i, j, k, 2),
+                                   c.avz(Sv, i, j, k), c.avz(Sv, i, j, k + 1));
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -403,6 +414,22 @@ __device__ __forceinline__ void add_linear(const Ctx &c, A &at) {
             }
         }
     }
+    if constexpr (DOF > DIM + 2) {
+        // salinity: sal * (S_xx + S_yy) - forward_average_S_y
+        // (Discretization.py:260-263; the 2D layout is the only one compiled)
+        static_assert(DIM == 2, "salinity is compiled for the 2D layout only");
+        constexpr int Sv = DIM + 2;
+        const double sal = c.p.sal;
+        Diff sx = second(rHx, rHpx, Dy, Dz), sy = second(rHy, rHpy, Dx, Dz);
+        add(ic<Sv>{}, ic<Sv>{}, ic<off1(0, 0)>{}, sal * sx.a0);
+        add(ic<Sv>{}, ic<Sv>{}, ic<off1(0, 2)>{}, sal * sx.a2);
+        add(ic<Sv>{}, ic<Sv>{}, ic<off1(1, 0)>{}, sal * sy.a0);
+        add(ic<Sv>{}, ic<Sv>{}, ic<off1(1, 2)>{}, sal * sy.a2);
+        add(ic<Sv>{}, ic<Sv>{}, ic<OC>{}, sal * (sx.a1 + sy.a1));
+        const double fa = Hpy * Dx * Dz / 2.0;
+        add(ic<1>{}, ic<Sv>{}, ic<off1(1, 1)>{}, 0.0 - fa);
+        add(ic<1>{}, ic<Sv>{}, ic<off1(1, 2)>{}, 0.0 - fa);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -484,7 +511,8 @@ __device__ __forceinline__ void wall_second_op(Atom<DIM, DOF, FONLY> &A) {
 
 template <int DIM, int DOF, bool FONLY, int a, bool high>
 __device__ __forceinline__ void force_op(Atom<DIM, DOF, FONLY> &A, double (&frc)[DOF], int var,
-                                         double fc, double ac) {
+                                         double fc, double ac, const double *prof = nullptr, int tcell = 0,
+                                         int plen = 0) {
     using AT = Atom<DIM, DOF, FONLY>;
     constexpr int out = high ? 2 : 0;
     static_for<DOF>([&](auto V) {
@@ -492,8 +520,19 @@ __device__ __forceinline__ void force_op(Atom<DIM, DOF, FONLY> &A, double (&frc)
         if (vv != var) return;
         double acc = 0.0;
         static_for<9>([&](auto Q) {
-            constexpr int s = AT::template S<vv, vv, off_q(a, out, decltype(Q)::value)>;
-            if constexpr (s >= 0) acc = acc + A.v[s] * fc;
+            constexpr int q = decltype(Q)::value;
+            constexpr int s = AT::template S<vv, vv, off_q(a, out, q)>;
+            if constexpr (s >= 0) {
+                if (prof) {
+                    // a profile along the first tangential axis (2D: the
+                    // second tangential offset is the centre)
+                    int m = tcell + q % 3 - 1;
+                    if (m < 0) m += plen;
+                    acc = acc + A.v[s] * (q / 3 == 1 ? prof[m] : 0.0);
+                } else {
+                    acc = acc + A.v[s] * fc;
+                }
+            }
         });
         frc[vv] = frc[vv] + acc;
         static_for<DOF>([&](auto D1) {
@@ -508,6 +547,34 @@ __device__ __forceinline__ void force_op(Atom<DIM, DOF, FONLY> &A, double (&frc)
                 }
             });
         });
+    });
+}
+
+// TF_BC_PIN (Discretization.py:690-702): entries coupling to var of cell
+// (0,0,0), periodic neighbours included, become 0; cell 0's row var gets -1
+// on its diagonal and no forcing.
+template <int DIM, int DOF, bool FONLY>
+__device__ __forceinline__ void pin_op(const Ctx &c, Atom<DIM, DOF, FONLY> &A, double (&frc)[DOF], int var) {
+    using AT = Atom<DIM, DOF, FONLY>;
+    const int nx = c.p.nx, ny = c.p.ny, nz = c.p.nz;
+    static_for<DOF>([&](auto V) {
+        constexpr int vv = decltype(V)::value;
+        if (vv != var) return;
+        static_for<DOF>([&](auto D1) {
+            static_for<27>([&](auto O) {
+                constexpr int d1 = decltype(D1)::value, o = decltype(O)::value;
+                constexpr int s = AT::template S<d1, vv, o>;
+                if constexpr (s >= 0) {
+                    const bool hit = (c.i + o % 3 - 1 + nx) % nx == 0 && (c.j + (o / 3) % 3 - 1 + ny) % ny == 0 &&
+                                     (c.k + o / 9 - 1 + nz) % nz == 0;
+                    if (hit) A.v[s] = 0.0;
+                }
+            });
+        });
+        if (c.i == 0 && c.j == 0 && c.k == 0) {
+            A.v[AT::template S<vv, vv, OC>] = -1.0;
+            frc[vv] = 0.0;
+        }
     });
 }
 
@@ -532,6 +599,19 @@ __device__ __forceinline__ void boundaries(const Ctx &c, Atom<DIM, DOF, FONLY> &
                 if (a == 0) wall_second_op<DIM, DOF, FONLY, 0>(A);
                 else if (a == 1) wall_second_op<DIM, DOF, FONLY, 1>(A);
                 else if constexpr (DIM > 2) wall_second_op<DIM, DOF, FONLY, 2>(A);
+            }
+        } else if (op.kind == TF_BC_PIN) {
+            pin_op<DIM, DOF, FONLY>(c, A, frc, op.var);
+        } else if (op.kind == TF_BC_FORCE_PROFILE) {
+            if constexpr (DIM == 2) {
+                if (on) {
+                    const double *prof = c.p.d_prof + (size_t)(int)op.fc * c.p.prof_len;
+                    const int tcell = a == 0 ? c.j : c.i;
+#define TF_FORCE(AX, HI) force_op<DIM, DOF, FONLY, AX, HI>(A, frc, op.var, 0.0, op.ac, prof, tcell, c.p.prof_len)
+                    if (a == 0) { if (op.high) TF_FORCE(0, true); else TF_FORCE(0, false); }
+                    else if (a == 1) { if (op.high) TF_FORCE(1, true); else TF_FORCE(1, false); }
+#undef TF_FORCE
+                }
             }
         } else if (on) {
 #define TF_FORCE(AX, HI) force_op<DIM, DOF, FONLY, AX, HI>(A, frc, op.var, op.fc, op.ac)
@@ -670,6 +750,7 @@ __global__ void mass_kernel(const tf_problem p, double *__restrict__ diag) {
     if constexpr (DIM == 3) o[2] = Hpz * Dy * Dx;
     o[DIM] = 0.0;
     if constexpr (DOF > DIM + 1) o[DIM + 1] = Dx * Dy * Dz;
+    if constexpr (DOF > DIM + 2) o[DIM + 2] = Dx * Dy * Dz;
 }
 
 template <int DIM, int DOF>
@@ -688,6 +769,17 @@ static int check_problem(const tf_problem *p) {
     if (p->nops < 0 || p->nops > TF_MAX_BC_OPS) return TF_ERR_ARG;
     if (p->metric_stride < p->nx || p->metric_stride < p->ny || p->metric_stride < p->nz) return TF_ERR_ARG;
     if ((int64_t)p->nx * p->ny * p->nz * 80 > INT32_MAX) return TF_ERR_SIZE;
+    for (int t = 0; t < p->nops; ++t) {
+        const tf_bc_op &op = p->ops[t];
+        if (op.kind == TF_BC_FORCE_PROFILE) {
+            if (p->dim != 2 || !p->d_prof || op.axis > 1) return TF_ERR_ARG;
+            const int along = op.axis == 0 ? p->ny : p->nx;
+            if (p->prof_len != along + 2 || !(op.fc >= 0 && op.fc < p->nprof)) return TF_ERR_ARG;
+        }
+        if ((op.kind == TF_BC_PIN || op.kind == TF_BC_FORCE || op.kind == TF_BC_FORCE_PROFILE) &&
+            (op.var < 0 || op.var >= p->dof))
+            return TF_ERR_ARG;
+    }
     return TF_OK;
 }
 

@@ -38,14 +38,16 @@ __host__ __device__ constexpr int off_index(int ox, int oy, int oz) { return ox 
 //   T row, T                     : star (diffusion + convection)
 //   T row, velocity b            : offset_b in {0,1}   (linearised T advection,
 //                                  Rayleigh-Benard perturbation term)
+//   velocity row a>=1, S; S row   : as for T (salinity: - forward average,
+//                                  diffusion + convection, linearised advection)
 // Every boundary fold moves offset 0/2 to 1 along its axis inside one
 // (d1, d2) pair, and each of these sets is closed under that projection.
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr bool in_template(int DIM, int DOF, int d1, int d2, int ox, int oy, int oz) {
     int o[3] = {ox, oy, oz};
     if (DIM == 2 && oz != 1) return false;
-    const int P = DIM, T = DIM + 1;
-    const bool hasT = DOF > DIM + 1;
+    const int P = DIM, T = DIM + 1, S = DIM + 2;
+    const bool hasT = DOF > DIM + 1, hasS = DOF > DIM + 2;
     int noncentre = (ox != 1) + (oy != 1) + (oz != 1);
     auto only = [&](int a, int lo, int hi) {
         for (int b = 0; b < 3; ++b) {
@@ -67,6 +69,7 @@ __host__ __device__ constexpr bool in_template(int DIM, int DOF, int d1, int d2,
         }
         if (d2 == P) return only(a, 1, 2);
         if (hasT && d2 == T) return a >= 1 && only(a, 1, 2);
+        if (hasS && d2 == S) return a >= 1 && only(a, 1, 2);
         return false;
     }
     if (d1 == P) {
@@ -74,8 +77,8 @@ __host__ __device__ constexpr bool in_template(int DIM, int DOF, int d1, int d2,
         if (d2 == P) return noncentre == 0;
         return false;
     }
-    if (hasT && d1 == T) {
-        if (d2 == T) return noncentre <= 1;
+    if ((hasT && d1 == T) || (hasS && d1 == S)) {
+        if (d2 == d1) return noncentre <= 1;
         if (d2 < DIM) return only(d2, 0, 1);
         return false;
     }
@@ -111,6 +114,7 @@ struct Layout {
     do {                                                              \
         if ((dim) == 2 && (dof) == 3) { CALL(2, 3); }                 \
         else if ((dim) == 2 && (dof) == 4) { CALL(2, 4); }            \
+        else if ((dim) == 2 && (dof) == 5) { CALL(2, 5); }            \
         else if ((dim) == 3 && (dof) == 4) { CALL(3, 4); }            \
         else if ((dim) == 3 && (dof) == 5) { CALL(3, 5); }            \
         else return TF_ERR_UNSUPPORTED;                               \

@@ -107,6 +107,7 @@ class BoundaryProgram:
         self.nx, self.ny, self.nz, self.dim, self.dof = nx, ny, nz, dim, dof
         self.x, self.y, self.z = x, y, z
         self.ops = []
+        self.profiles = []
 
     # walls
     def _wall(self, axis, high, sign):
@@ -114,8 +115,22 @@ class BoundaryProgram:
 
     def _force(self, axis, high, var, fc, ac):
         if np.ndim(fc) != 0:
-            raise NotImplementedError('spatially varying boundary forcing is not supported on the GPU')
+            # a forcing that varies along the face: numpy.ones((n1 + 2, n2 + 2))
+            # * value as BoundaryConditions._constant_forcing broadcasts it;
+            # in 2D only its column 0 (the centre of the second tangential
+            # axis) multiplies nonzero entries
+            if self.dim != 2 or axis > 1:
+                raise NotImplementedError('varying boundary forcing is supported on 2D x/y faces only')
+            n1 = self.ny if axis == 0 else self.nx
+            n2 = self.nz
+            prof = (np.ones((n1 + 2, n2 + 2)) * fc)[:, 0]
+            self.ops.append((_lib.TF_BC_FORCE_PROFILE, axis, int(high), var, float(len(self.profiles)), float(ac)))
+            self.profiles.append(np.ascontiguousarray(prof, dtype=np.float64))
+            return
         self.ops.append((_lib.TF_BC_FORCE, axis, int(high), var, float(fc), float(ac)))
+
+    def _pin(self, var):
+        self.ops.append((_lib.TF_BC_PIN, 0, 0, var, 0.0, 0.0))
 
     def no_slip_east(self, atom=None): self._wall(0, True, -1)
     def no_slip_west(self, atom=None): self._wall(0, False, -1)
@@ -187,14 +202,29 @@ class BoundaryProgram:
     def heat_flux_top(self, atom, q, biot=0.0): self._heat_flux(2, True, q, biot)
     def heat_flux_bottom(self, atom, q, biot=0.0): self._heat_flux(2, False, q, biot)
 
+    # salinity flux (BoundaryConditions.py:423-469)
+    def _salinity_flux(self, axis, high, q):
+        c, n = self._coord(axis)
+        if high:
+            self._force(axis, True, self.dim + 2, (c[n] - c[n - 2]) / 2 * q, 1)
+        else:
+            self._force(axis, False, self.dim + 2, -((c[0] - c[-2]) / 2) * q, 1)
+
+    def salinity_flux_east(self, atom, q): self._salinity_flux(0, True, q)
+    def salinity_flux_west(self, atom, q): self._salinity_flux(0, False, q)
+    def salinity_flux_north(self, atom, q): self._salinity_flux(1, True, q)
+    def salinity_flux_south(self, atom, q): self._salinity_flux(1, False, q)
+    def salinity_flux_top(self, atom, q): self._salinity_flux(2, True, q)
+    def salinity_flux_bottom(self, atom, q): self._salinity_flux(2, False, q)
+
     def get_forcing(self):
         return None
 
 
 def builtin_boundaries(parameters, bc, dim, nz):
     """The call sequences of Discretization._lid_driven_cavity,
-    _rayleigh_benard, _differentially_heated_cavity and _double_gyre
-    (Discretization.py:577-655)."""
+    _rayleigh_benard, _differentially_heated_cavity, _double_gyre and _amoc
+    (Discretization.py:577-702)."""
     problem = parameters.get('Problem Type', 'Lid-driven Cavity').lower()
     if problem == 'lid-driven cavity':
         v = get_parameter(parameters, 'Lid Velocity', 1)
@@ -236,6 +266,22 @@ def builtin_boundaries(parameters, bc, dim, nz):
         bc.no_slip_west()
         bc.free_slip_north()
         bc.free_slip_south()
+    elif problem == 'amoc':
+        # Discretization._amoc (Discretization.py:657-702)
+        bc.heat_flux_east(None, 0)
+        bc.heat_flux_west(None, 0)
+        bc.salinity_flux_east(None, 0)
+        bc.salinity_flux_west(None, 0)
+        bc.free_slip_east()
+        bc.free_slip_west()
+        bc.heat_flux_south(None, 0)
+        bc.salinity_flux_south(None, 0)
+        bc.free_slip_south()
+        T_S, Q_S = amoc_profiles(parameters, bc.x, bc.nx, bc.nz)
+        bc.temperature_north(None, get_parameter(parameters, 'Temperature Forcing') * T_S)
+        bc.salinity_flux_north(None, get_parameter(parameters, 'Freshwater Flux') * Q_S)
+        bc.free_slip_north()
+        bc._pin(dim + 2)
     elif problem == 'differentially heated cavity':
         bc.temperature_east(None, -1 / 2)
         bc.temperature_west(None, 1 / 2)
@@ -263,14 +309,16 @@ def scalars(parameters, dim, dof, nz):
     rossby = get_parameter(parameters, 'Rossby Parameter')
     if rossby and dim != 2:
         raise NotImplementedError('the Coriolis term exists in 2D only (Discretization.py:253-255)')
-    if dof > dim + 2:
-        raise NotImplementedError('salinity is not available on the GPU backend')
+    if dof > dim + 2 and dim != 2:
+        raise NotImplementedError('salinity is compiled for 2D grids only')
     if Re == 0:
         Re = 1
     if Gr == 0:
         Gr = 1 / Pr
     visc = 1 / (Re * np.sqrt(Gr))
     cond = 1 / (Pr * np.sqrt(Gr))
+    Le = get_parameter(parameters, 'Lewis Number', 1.0)
+    sal = 1 / (Le * Pr * np.sqrt(Gr))
     nonlinear = not (get_parameter(parameters, 'Reynolds Number') == 0 and not dof > dim + 1)
     buoy_row = -1
     if dof > dim + 1:
@@ -286,7 +334,23 @@ def scalars(parameters, dim, dof, nz):
         wind = get_parameter(parameters, 'Wind Stress Parameter') / (2 * np.pi)
     return dict(visc=float(visc), cond=float(cond), nonlinear=int(nonlinear),
                 buoy_row=buoy_row, biot_row=biot_row, biot=float(biot), rossby=float(rossby),
-                wind=float(wind), asym=float(get_parameter(parameters, 'Asymmetry Parameter')))
+                wind=float(wind), asym=float(get_parameter(parameters, 'Asymmetry Parameter')), sal=float(sal))
+
+
+def amoc_profiles(parameters, x, nx, nz):
+    """T_S and Q_S of Discretization._amoc (Discretization.py:674-689) over
+    the cell centres, shape (nx + 2, nz + 2), set in column 0."""
+    xc = np.zeros(len(x) - 1)
+    for m in range(-1, len(x) - 2):
+        xc[m] = (x[m] + x[m - 1]) / 2
+    asym = get_parameter(parameters, 'Asymmetry Parameter')
+    A = parameters.get('X-max', 1.0)
+    T_S = np.zeros((nx + 2, nz + 2))
+    T_S[:, 0] = 1 / 2 * ((1 - asym) * np.cos(2 * np.pi * (xc / A - 1 / 2)) + asym * np.cos(np.pi * xc / A) + 1)
+    p = 2
+    Q_S = np.zeros((nx + 2, nz + 2))
+    Q_S[:, 0] = 3 * np.cos(p * np.pi * (xc / A - 1 / 2)) - 6 / (p * np.pi) * np.sin(p * np.pi / 2)
+    return T_S, Q_S
 
 
 def aux_table(y, ny):
@@ -300,7 +364,7 @@ def aux_table(y, ny):
 
 
 def make_problem(parameters, nx, ny, nz, dim, dof, x, y, z, d_metric, stride, boundary_conditions=None,
-                 d_aux=None):
+                 d_aux=None, upload_profiles=None):
     """Fill the tf_problem structure for the current parameter values
     (d_aux: device copy of aux_table(y, ny), needed for the Coriolis term and
     the wind stress)."""
@@ -327,4 +391,12 @@ def make_problem(parameters, nx, ny, nz, dim, dof, x, y, z, d_metric, stride, bo
     if (p.rossby or p.wind) and not d_aux:
         raise ValueError('the Coriolis term and the wind stress need the aux table')
     p.d_aux = d_aux
+    p.sal = sc['sal']
+    if bc.profiles:
+        if upload_profiles is None:
+            raise ValueError('varying boundary forcing needs a profile upload')
+        table = np.stack(bc.profiles)
+        p.d_prof = upload_profiles(table)
+        p.prof_len = table.shape[1]
+        p.nprof = table.shape[0]
     return p

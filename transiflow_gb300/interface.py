@@ -9,7 +9,8 @@ provides the methods the drivers call -- ``vector``, ``rhs``, ``jacobian``,
 ``array_from_vector`` -- so ``Continuation`` and ``TimeIntegration`` run on
 it unchanged.  States live on the GPU as :class:`DeviceVector`; the
 discretisation, the Jacobian and the solves run in libtfcuda kernels.
-``eigs`` is not provided (docs/custom-backend.rst allows that).
+``eigs`` computes the eigenvalues nearest a real target by shift-and-invert
+Arnoldi with the GPU solver.
 
 Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
   'Factor Precision'  'fp64' (default) or 'fp32' for the preconditioner LU
@@ -90,6 +91,7 @@ class Interface:
         self._metric = torch.as_tensor(table.ravel()).to(self.device)
         self._stride = table.shape[2]
         self._aux = torch.as_tensor(grid.aux_table(self.y, ny).ravel()).to(self.device)
+        self._prof = None
         # validate the problem type and boundary program now
         self._problem()
         # pattern of the stencil CSR
@@ -136,7 +138,17 @@ class Interface:
     def _problem(self):
         return grid.make_problem(self.parameters, self.nx, self.ny, self.nz, self.dim, self.dof,
                                  self.x, self.y, self.z, self._metric.data_ptr(), self._stride,
-                                 self.boundary_conditions, self._aux.data_ptr())
+                                 self.boundary_conditions, self._aux.data_ptr(), self._upload_profiles)
+
+    def _upload_profiles(self, table):
+        """Device copy of the boundary forcing profiles (they depend on the
+        parameters, so every assembly refreshes them; the copy is ordered on
+        the current stream before the kernels that read it)."""
+        t = torch.as_tensor(np.ascontiguousarray(table.ravel()))
+        if self._prof is None or self._prof.numel() != t.numel():
+            self._prof = torch.empty(t.numel(), dtype=torch.float64, device=self.device)
+        self._prof.copy_(t)
+        return self._prof.data_ptr()
 
     # -- vectors -----------------------------------------------------------------
     def vector(self):
@@ -208,7 +220,46 @@ class Interface:
         return (y.numpy() if host else y), y2
 
     def eigs(self, state, return_eigenvectors=False, enable_recycling=False):
-        raise NotImplementedError('the CUDA backend has no eigenvalue solver')
+        """Generalised eigenvalues of J(u, p) v = lambda M v closest to the
+        target (the contract of BaseInterface.eigs, BaseInterface.py:355-386),
+        by shift-and-invert Arnoldi: ARPACK through scipy.sparse.linalg.eigs,
+        as the reference's tests compute them (tests/jada_fixtures.py:72-87),
+        on the operator (J - sigma M)^-1 M, whose every application is one
+        solve with the GPU factorisation of the gauged J - sigma M.
+        'Eigenvalue Solver' options: 'Number of Eigenvalues' (5), 'Target'
+        (0, real), 'Tolerance' (1e-7).  The eigenvalues are ordered as the
+        reference orders them: largest real part first, real parts >= 100
+        last.  enable_recycling is accepted and ignored."""
+        import scipy.sparse.linalg as sla
+        opts = self.parameters.get('Eigenvalue Solver', {})
+        num = int(opts.get('Number of Eigenvalues', 5))
+        target = complex(opts.get('Target', 0.0))
+        if target.imag != 0:
+            raise NotImplementedError('complex eigenvalue targets')
+        sigma = target.real
+        tol = float(opts.get('Tolerance', 1e-7))
+        x = state if isinstance(state, DeviceVector) else self.vector_from_array(state)
+        J = self.jacobian(x)
+        M = self.mass_matrix()
+        A = J - M * sigma if sigma != 0 else J
+
+        def op(v):
+            b = M @ DeviceVector.from_array(np.ascontiguousarray(np.real(v), dtype=np.float64), self.device)
+            return self.solve(A, b).numpy()
+
+        n = self.n
+        OP = sla.LinearOperator((n, n), matvec=op, dtype=np.float64)
+        v0 = np.random.default_rng(0).standard_normal(n)
+        k = min(num, n - 2)
+        if return_eigenvectors:
+            mu, V = sla.eigs(OP, k=k, which='LM', tol=tol, v0=v0)
+        else:
+            mu = sla.eigs(OP, k=k, which='LM', tol=tol, v0=v0, return_eigenvectors=False)
+        lam = sigma + 1 / mu
+        order = sorted(range(len(lam)), key=lambda i: -lam[i].real if lam[i].real < 100 else 100)
+        if return_eigenvectors:
+            return lam[order][:num], V[:, order][:, :num]
+        return lam[order][:num]
 
     # -- checkpointing (BaseInterface.py:118-215) ---------------------------------
     def save_json(self, name, obj):
