@@ -255,6 +255,11 @@ def fp64_peak():
     return 2.0 * 4096 ** 3 / best / 1e12
 
 
+# DRAM bytes (read + write) of one factorisation, summed over its launches in
+# one ncu capture of `bench.py --profile factor` on a GB300.
+FACTOR_TRAFFIC = {(256, 1, 'fp64'): 6.046e9}
+
+
 def roofline(itf, x, args, lib):
     """Live CUDA-event timing of the dominant kernels over rotating buffers
     larger than L2 (129 MB)."""
@@ -336,7 +341,10 @@ def roofline(itf, x, args, lib):
             'achieved': a, 'peak': f64 if args.precision == 'fp64' else None, 'unit': 'TFLOP/s',
             'frac': a / f64 if args.precision == 'fp64' else None,
             'peak_source': 'FP64 dense GEMM of this GPU measured in this run (cuBLAS DGEMM 4096^3)',
-            'traffic': None, 'algorithmic_flops': flops, 'hbm_peak_gbs': peak,
+            'traffic': FACTOR_TRAFFIC.get((args.nx, args.nz, args.precision)),
+            'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum over the launches of one '
+                              'factorisation (caches flushed per kernel: an upper bound)',
+            'algorithmic_flops': flops, 'hbm_peak_gbs': peak,
             'hbm_peak_source': '%s (MEASURED_PEAKS.json hbm_gbs)' % which, 'kernels': kernels}
 
 

@@ -263,6 +263,25 @@ int tf_nd_solve_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_
 int tf_nd_solve_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,
                     double *d_x, tf_stream_t stream);
 
+/* Replaces, in place, the factored own blocks L11 and U11 of every front by
+ * their inverses (recursive halving, batched GEMMs), so that tf_nd_solve_inv_*
+ * applies the factors without sequential substitution.  Call after
+ * tf_nd_factor_* on the same fronts; the fronts are then usable only with
+ * tf_nd_solve_inv_*.  d_work: tf_nd_invert_workspace_bytes(plan, sizeof
+ * element) bytes of device scratch.  No counterpart in the reference (its
+ * SuperLU solve substitutes, SciPy.py:194-202).                              */
+size_t tf_nd_invert_workspace_bytes(const tf_nd_plan *plan, int elem_size);
+int tf_nd_invert_f64(const tf_nd_plan *plan, double *d_fronts, double *d_work, size_t work_bytes,
+                     tf_stream_t stream);
+int tf_nd_invert_f32(const tf_nd_plan *plan, float *d_fronts, float *d_work, size_t work_bytes,
+                     tf_stream_t stream);
+/* In-place solve with inverted own blocks (after tf_nd_invert_*): d_x as in
+ * tf_nd_solve_*; d_scratch: plan->n doubles of device scratch.              */
+int tf_nd_solve_inv_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_t *d_piv,
+                        double *d_x, double *d_scratch, tf_stream_t stream);
+int tf_nd_solve_inv_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,
+                        double *d_x, double *d_scratch, tf_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

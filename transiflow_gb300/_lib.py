@@ -21,7 +21,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), 'include')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 # the assembly TU keeps the reference's separate multiply/add rounding
 SOURCES = [('tf_assemble.cu', ['-fmad=false']), ('tf_sparse.cu', []), ('tf_nd.cu', []), ('tf_nd_panel_f32.cu', []),
-           ('tf_nd_panel_f64.cu', [])]
+           ('tf_nd_panel_f64.cu', []),
+           ('tf_nd_inv.cu', [])]
 
 TF_MAX_BC_OPS = 24
 TF_METRIC_FIELDS = 10
@@ -125,6 +126,11 @@ _SIGNATURES = {
     'tf_nd_factor_f32': ([_P, _P, _P, _P, _P, _P], _I),
     'tf_nd_solve_f64': ([_P, _P, _P, _P, _P], _I),
     'tf_nd_solve_f32': ([_P, _P, _P, _P, _P], _I),
+    'tf_nd_invert_workspace_bytes': ([_P, _I], ctypes.c_size_t),
+    'tf_nd_invert_f64': ([_P, _P, _P, ctypes.c_size_t, _P], _I),
+    'tf_nd_invert_f32': ([_P, _P, _P, ctypes.c_size_t, _P], _I),
+    'tf_nd_solve_inv_f64': ([_P, _P, _P, _P, _P, _P], _I),
+    'tf_nd_solve_inv_f32': ([_P, _P, _P, _P, _P, _P], _I),
 }
 
 _lib = None

@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(GEMV_THREADS) bnd_kernel(DevPlan P, int node0,
     if (r0 + lane < rhi) atomicAdd(x + g[r0 + lane], -(double)s);
 }
 
-static DevPlan dev_plan(const tf_nd_plan *p, const int32_t *rank) {
+DevPlan dev_plan(const tf_nd_plan *p, const int32_t *rank) {
     DevPlan d;
     d.n_own = p->d_n_own;
     d.f = p->d_f;
@@ -432,7 +432,7 @@ static DevPlan dev_plan(const tf_nd_plan *p, const int32_t *rank) {
     return d;
 }
 
-static int check_plan(const tf_nd_plan *p) {
+int check_plan(const tf_nd_plan *p) {
     if (!p || p->n <= 0 || p->nnodes <= 0 || p->nlevels <= 0 || !p->level_ptr || !p->max_own || !p->max_f)
         return TF_ERR_ARG;
     if (!p->d_n_own || !p->d_f || !p->d_parent || !p->d_front_off || !p->d_idx_off || !p->d_idx ||
@@ -551,8 +551,7 @@ static int tri(const DevPlan &D, int node0, int cnt, int mo, int nsm, const T *f
 }
 
 template <typename T, bool FWD>
-static void launch_bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, const T *fronts, double *x,
-                       cudaStream_t s) {
+void bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, const T *fronts, double *x, cudaStream_t s) {
     if (rows <= 0 || cols <= 0) return;
     dim3 grid((rows + GEMV_ROWS - 1) / GEMV_ROWS, cnt, (cols + GEMV_COLS - 1) / GEMV_COLS);
     bnd_kernel<T, FWD><<<grid, GEMV_THREADS, sizeof(T) * 2 * GEMV_WARPS * TILE, s>>>(D, node0, fronts, x);
@@ -576,17 +575,22 @@ static int solve(const tf_nd_plan *p, const T *fronts, const int32_t *piv, doubl
         const int mo = p->max_own[h], mf = p->max_f[h];
         if (cnt <= 0 || mo <= 0) continue;
         if ((e = tri<T, true>(D, node0, cnt, mo, nsm, fronts, piv, x, s))) return e;
-        launch_bnd<T, true>(D, node0, cnt, mf, mo, fronts, x, s);
+        bnd<T, true>(D, node0, cnt, mf, mo, fronts, x, s);
     }
     for (int h = p->nlevels - 1; h >= 0; --h) {
         const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
         const int mo = p->max_own[h], mf = p->max_f[h];
         if (cnt <= 0 || mo <= 0) continue;
-        launch_bnd<T, false>(D, node0, cnt, mo, mf, fronts, x, s);
+        bnd<T, false>(D, node0, cnt, mo, mf, fronts, x, s);
         if ((e = tri<T, false>(D, node0, cnt, mo, nsm, fronts, piv, x, s))) return e;
     }
     return cuda_status();
 }
+
+template void bnd<float, true>(const DevPlan &, int, int, int, int, const float *, double *, cudaStream_t);
+template void bnd<float, false>(const DevPlan &, int, int, int, int, const float *, double *, cudaStream_t);
+template void bnd<double, true>(const DevPlan &, int, int, int, int, const double *, double *, cudaStream_t);
+template void bnd<double, false>(const DevPlan &, int, int, int, int, const double *, double *, cudaStream_t);
 
 }  // namespace nd
 }  // namespace tf

@@ -30,6 +30,14 @@ __device__ __forceinline__ T tabs(T x) { return x < T(0) ? -x : x; }
 // (TF_ERR_SIZE when static plus dynamic shared memory would not fit).
 int ensure_smem(const void *kernel, size_t bytes);
 
+DevPlan dev_plan(const tf_nd_plan *p, const int32_t *rank);
+int check_plan(const tf_nd_plan *p);
+
+// x[bnd] -= L21 y (FWD) or x[own] -= U12 x[bnd] for every front of one tree
+// height (rows x cols at most per front).
+template <typename T, bool FWD>
+void bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, const T *fronts, double *x, cudaStream_t s);
+
 // Pivoted LU of the 32-column panel at column k of every front of one tree
 // height (node0 .. node0+cnt-1, at most `rows` panel rows), including the
 // row swaps of the columns outside the panel.

@@ -1,0 +1,363 @@
+// Explicit inverses of the factored own blocks (L11 unit lower, U11 upper)
+// of every front, and the preconditioner application that uses them.
+//
+// Applying L11^-1 and U11^-1 by substitution is a chain of dependent 32-row
+// block steps; on GB300, where a warp-wide FP64 instruction occupies an SM
+// sub-partition for about 64 cycles, each step costs microseconds and the
+// chains of the large fronts near the root dominate an application.  Both
+// triangles are therefore inverted once per factorisation (in place: the
+// inverse of the unit lower part keeps the strictly lower positions, the
+// inverse of the upper part the upper ones), and an application becomes a
+// gather plus a triangular matrix-vector product per tree height, parallel
+// over all rows.
+//
+// Inversion by recursive halving of each own block: a segment of m rows
+// (m > 32) splits at m1 = 32 ceil(nb / 2) (nb = ceil(m / 32) row blocks),
+//   L = [A 0; B C]:  L^-1 = [A^-1 0; -C^-1 B A^-1  C^-1]
+//   U = [A B; 0 C]:  U^-1 = [A^-1  -A^-1 B C^-1; 0 C^-1]
+// The 32-row diagonal blocks are inverted first (one warp each, column by
+// column), then the off-diagonal blocks are combined from the deepest split
+// up, two GEMMs per split (T = B X, B <- -Y T), batched over all splits of
+// one depth and all fronts of one height.  The extra work is about n^3 / 3
+// flops per triangle of an n-row own block.
+
+#include "tf_nd.cuh"
+
+#include <algorithm>
+
+namespace tf {
+namespace nd {
+
+constexpr int IB = 32;        // diagonal block size
+constexpr int IT = 64;        // GEMM tile
+constexpr int IK = 32;        // GEMM k chunk
+constexpr int ITHREADS = 256;
+
+__host__ __device__ constexpr int split_at(int m) { return IB * ((((m + IB - 1) / IB) + 1) / 2); }
+
+// Scratch row stride for the products of a front with up to n own rows.
+__host__ __device__ constexpr int inv_ld(int n) { return n > IB ? split_at(n) : 1; }
+
+// Number of split depths of an n-row block (0 for a single 32-row block).
+static int inv_depths(int n) {
+    int d = 0;
+    for (int nb = (n + IB - 1) / IB; nb > 1; nb = (nb + 1) / 2) ++d;
+    return d;
+}
+
+// Segment of split node q at depth d; false when that node does not exist
+// (a leaf was reached above it) or is a single block.
+__device__ __forceinline__ bool split_node(int n, int depth, int q, int &r0, int &m) {
+    r0 = 0;
+    m = n;
+    for (int d = depth - 1; d >= 0; --d) {
+        if (m <= IB) return false;
+        const int m1 = split_at(m);
+        if ((q >> d) & 1) { r0 += m1; m -= m1; } else { m = m1; }
+    }
+    return m > IB;
+}
+
+// Invert the 32 x 32 diagonal blocks of every front of one height in place:
+// the unit lower part (column j solves L x = e_j forwards, lane = column) and
+// the upper part (U x = e_j backwards).  One warp per block.
+template <typename T>
+__global__ void __launch_bounds__(32) inv_diag_kernel(DevPlan P, int node0, T *fronts) {
+    __shared__ T D[IB][IB + 1];
+    __shared__ T X[IB][IB + 1];
+    const int node = node0 + blockIdx.y;
+    const int n = P.n_own[node], f = P.f[node];
+    const int b0 = blockIdx.x * IB;
+    if (b0 >= n) return;
+    const int nb = min(IB, n - b0);
+    T *F = fronts + P.front_off[node] + (size_t)b0 * f + b0;
+    const int lane = threadIdx.x;
+    for (int i = 0; i < IB; ++i) D[i][lane] = (i < nb && lane < nb) ? F[(size_t)i * f + lane] : T(0);
+    __syncwarp();
+    // lower: x_i = [i == j] - sum_{t < i} L_it x_t
+    for (int i = 0; i < IB; ++i) {
+        T s = i == lane ? T(1) : T(0);
+        for (int t = 0; t < i; ++t) s -= D[i][t] * X[t][lane];
+        X[i][lane] = s;
+    }
+    __syncwarp();
+    for (int i = 0; i < nb; ++i)
+        if (lane < i) F[(size_t)i * f + lane] = X[i][lane];
+    __syncwarp();
+    // upper: x_i = ([i == j] - sum_{t > i} U_it x_t) / U_ii
+    for (int i = IB - 1; i >= 0; --i) {
+        T s = i == lane ? T(1) : T(0);
+        for (int t = i + 1; t < IB; ++t) s -= D[i][t] * X[t][lane];
+        const T d = i < nb ? D[i][i] : T(1);
+        X[i][lane] = s / d;
+    }
+    __syncwarp();
+    for (int i = 0; i < nb; ++i)
+        if (lane >= i && lane < nb) F[(size_t)i * f + lane] = X[i][lane];
+}
+
+// One GEMM of the recursive combination at split depth `depth` for every
+// front of one height (grid: output tiles x split nodes x fronts):
+//   UPPER = false, STAGE 0:  T = B A^-1        (m2 x m1, A^-1 unit lower)
+//                  STAGE 1:  B = -C^-1 T       (C^-1 unit lower)
+//   UPPER = true,  STAGE 0:  T = B C^-1        (m1 x m2, C^-1 upper)
+//                  STAGE 1:  B = -A^-1 T       (A^-1 upper)
+// with A = rows/cols [r0, r0+m1), C = [r0+m1, r0+m) of the node's segment,
+// T in the front's scratch rows r0.. (row stride ld).  The triangular
+// operand's zero half is skipped along k.
+template <typename T, bool UPPER, int STAGE>
+__global__ void __launch_bounds__(ITHREADS) inv_gemm_kernel(DevPlan P, int node0, int depth, T *fronts, T *work,
+                                                            int ld, int64_t front_stride) {
+    const int node = node0 + blockIdx.z;
+    const int n = P.n_own[node], f = P.f[node];
+    int r0, m;
+    if (!split_node(n, depth, blockIdx.y, r0, m)) return;
+    const int m1 = split_at(m), m2 = m - m1;
+    T *F = fronts + P.front_off[node];
+    T *W = work + (int64_t)blockIdx.z * front_stride;
+    // output M x N, inner K; operand accessors
+    const int M = UPPER ? m1 : m2, N = UPPER ? m2 : m1, K = STAGE == 0 ? N : M;
+    const int tiles_n = (N + IT - 1) / IT;
+    const int tm = blockIdx.x / tiles_n, tn = blockIdx.x % tiles_n;
+    const int i0 = tm * IT, j0 = tn * IT;
+    if (i0 >= M) return;
+    // k range with a nonzero triangular operand
+    int klo = 0, khi = K;
+    if (STAGE == 0) {        // (dense X) x (triangular Y): Y[k][j] nonzero for k >= j (lower) / k <= j (upper)
+        if (UPPER) khi = min(K, j0 + IT); else klo = j0;
+    } else {                 // (triangular Y) x (dense T): Y[i][k] nonzero for k <= i (lower) / k >= i (upper)
+        if (UPPER) klo = i0; else khi = min(K, i0 + IT);
+    }
+    __shared__ T As[IK][IT + 1];   // As[k][i]
+    __shared__ T Bs[IK][IT + 1];   // Bs[k][j]
+    const int tr = (threadIdx.x / 16) * 4, tc = (threadIdx.x % 16) * 4;
+    T acc[4][4] = {};
+    for (int k0 = klo - (klo % IK); k0 < khi; k0 += IK) {
+        for (int t = threadIdx.x; t < IK * IT; t += ITHREADS) {
+            const int kk = t % IK, ii = t / IK;   // A tile: consecutive threads along k
+            const int i = i0 + ii, k = k0 + kk;
+            T a = T(0);
+            if (i < M && k < K && k >= klo && k < khi) {
+                if (STAGE == 0) {
+                    a = UPPER ? F[(size_t)(r0 + i) * f + r0 + m1 + k] : F[(size_t)(r0 + m1 + i) * f + r0 + k];
+                } else {
+                    // triangular Y = (lower) C^-1 at [r0+m1, r0+m1) or (upper) A^-1 at [r0, r0)
+                    const int base = UPPER ? r0 : r0 + m1;
+                    if (UPPER) a = k > i ? F[(size_t)(base + i) * f + base + k] : (k == i ? F[(size_t)(base + i) * f + base + k] : T(0));
+                    else a = k < i ? F[(size_t)(base + i) * f + base + k] : (k == i ? T(1) : T(0));
+                }
+            }
+            As[kk][ii] = a;
+        }
+        for (int t = threadIdx.x; t < IK * IT; t += ITHREADS) {
+            const int jj = t % IT, kk = t / IT;   // B tile: consecutive threads along j
+            const int j = j0 + jj, k = k0 + kk;
+            T b = T(0);
+            if (j < N && k < K && k >= klo && k < khi) {
+                if (STAGE == 0) {
+                    // triangular Y = (lower) A^-1 at [r0, r0) or (upper) C^-1 at [r0+m1, r0+m1)
+                    const int base = UPPER ? r0 + m1 : r0;
+                    if (UPPER) b = k <= j ? F[(size_t)(base + k) * f + base + j] : T(0);
+                    else b = k > j ? F[(size_t)(base + k) * f + base + j] : (k == j ? T(1) : T(0));
+                } else {
+                    b = W[(int64_t)(r0 + k) * ld + j];   // T (K x N) in scratch rows r0..
+                }
+            }
+            Bs[kk][jj] = b;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < IK; ++kk) {
+            T a[4], b[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) { a[u] = As[kk][tr + u]; b[u] = Bs[kk][tc + u]; }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] += a[u] * b[v];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int i = i0 + tr + u;
+        if (i >= M) continue;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const int j = j0 + tc + v;
+            if (j >= N) continue;
+            if (STAGE == 0)
+                W[(int64_t)(r0 + i) * ld + j] = acc[u][v];
+            else if (UPPER)
+                F[(size_t)(r0 + i) * f + r0 + m1 + j] = -acc[u][v];
+            else
+                F[(size_t)(r0 + m1 + i) * f + r0 + j] = -acc[u][v];
+        }
+    }
+}
+
+static size_t invert_work_elems(const tf_nd_plan *p) {
+    size_t w = 0;
+    for (int h = 0; h < p->nlevels; ++h) {
+        const int cnt = p->level_ptr[h + 1] - p->level_ptr[h], mo = p->max_own[h];
+        if (cnt > 0 && mo > IB) w = std::max(w, (size_t)cnt * (size_t)mo * (size_t)inv_ld(mo));
+    }
+    return w;
+}
+
+template <typename T>
+static int invert(const tf_nd_plan *p, const DevPlan &D, T *fronts, T *work, size_t work_bytes, cudaStream_t s) {
+    if (work_bytes < invert_work_elems(p) * sizeof(T)) return TF_ERR_ARG;
+    for (int h = 0; h < p->nlevels; ++h) {
+        const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
+        const int mo = p->max_own[h];
+        if (cnt <= 0 || mo <= 0) continue;
+        inv_diag_kernel<T><<<dim3((mo + IB - 1) / IB, cnt), 32, 0, s>>>(D, node0, fronts);
+        launched();
+        const int ld = inv_ld(mo);
+        const int64_t stride = (int64_t)mo * ld;
+        for (int depth = inv_depths(mo) - 1; depth >= 0; --depth) {
+            // the largest node at this depth has at most split_at(mo >> depth)-ish rows; bound the
+            // tile grid by the root's halves
+            const int half = split_at(mo);
+            const int tiles = ((half + IT - 1) / IT) * ((half + IT - 1) / IT);
+            dim3 g(tiles, 1 << depth, cnt);
+            inv_gemm_kernel<T, false, 0><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+            launched();
+            inv_gemm_kernel<T, false, 1><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+            launched();
+            inv_gemm_kernel<T, true, 0><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+            launched();
+            inv_gemm_kernel<T, true, 1><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+            launched();
+        }
+    }
+    return cuda_status();
+}
+
+// ---------------------------------------------------------------------------
+// Application with the inverted blocks.
+// ---------------------------------------------------------------------------
+constexpr int VT = 128;   // rows per CTA of the triangular products
+
+// scratch[g[c]] = x[g[pv[c]]] (forward, with the row permutation) or
+// x[g[c]] (backward) for the own rows of every front of one height.
+template <bool FWD>
+__global__ void __launch_bounds__(VT) inv_gather_kernel(DevPlan P, int node0, const int32_t *piv, const double *x,
+                                                        double *scratch) {
+    const int node = node0 + blockIdx.y;
+    const int n = P.n_own[node];
+    const int c = blockIdx.x * VT + threadIdx.x;
+    if (c >= n) return;
+    const int32_t *g = P.idx + P.idx_off[node];
+    scratch[g[c]] = FWD ? x[g[piv[P.piv_off[node] + c]]] : x[g[c]];
+}
+
+// x[g[r]] = (L11^-1 s)_r (forward; unit diagonal) or (U11^-1 s)_r
+// (backward) for the own rows, s = scratch[g[.]] staged in shared memory;
+// one row per thread streaming through the L1 cache.
+template <typename T, bool FWD>
+__global__ void __launch_bounds__(VT) inv_apply_kernel(DevPlan P, int node0, const T *fronts, const double *scratch,
+                                                       double *x) {
+    extern __shared__ unsigned char smem_raw[];
+    T *sv = reinterpret_cast<T *>(smem_raw);
+    const int node = node0 + blockIdx.y;
+    const int n = P.n_own[node], f = P.f[node];
+    if (blockIdx.x * VT >= n) return;
+    const int32_t *g = P.idx + P.idx_off[node];
+    for (int c = threadIdx.x; c < n; c += VT) sv[c] = (T)scratch[g[c]];
+    __syncthreads();
+    const int r = blockIdx.x * VT + threadIdx.x;
+    if (r >= n) return;
+    const T *row = fronts + P.front_off[node] + (size_t)r * f;
+    const int c0 = FWD ? 0 : r, c1 = FWD ? r : n;
+    T s0 = FWD ? sv[r] : T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+    int c = c0;
+    for (; c + 4 <= c1; c += 4) {
+        s0 += __ldg(row + c) * sv[c];
+        s1 += __ldg(row + c + 1) * sv[c + 1];
+        s2 += __ldg(row + c + 2) * sv[c + 2];
+        s3 += __ldg(row + c + 3) * sv[c + 3];
+    }
+    for (; c < c1; ++c) s0 += __ldg(row + c) * sv[c];
+    x[g[r]] = (double)((s0 + s1) + (s2 + s3));
+}
+
+template <typename T>
+static int solve_inv(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int32_t *piv, double *x,
+                     double *scratch, cudaStream_t s) {
+    size_t mo_all = 0;
+    for (int h = 0; h < p->nlevels; ++h) mo_all = std::max(mo_all, (size_t)p->max_own[h]);
+    int e = ensure_smem((const void *)inv_apply_kernel<T, true>, sizeof(T) * mo_all);
+    if (!e) e = ensure_smem((const void *)inv_apply_kernel<T, false>, sizeof(T) * mo_all);
+    if (e) return e;
+    for (int h = 0; h < p->nlevels; ++h) {
+        const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
+        const int mo = p->max_own[h], mf = p->max_f[h];
+        if (cnt <= 0 || mo <= 0) continue;
+        const dim3 g((mo + VT - 1) / VT, cnt);
+        inv_gather_kernel<true><<<g, VT, 0, s>>>(D, node0, piv, x, scratch);
+        launched();
+        inv_apply_kernel<T, true><<<g, VT, sizeof(T) * mo, s>>>(D, node0, fronts, scratch, x);
+        launched();
+        bnd<T, true>(D, node0, cnt, mf, mo, fronts, x, s);
+    }
+    for (int h = p->nlevels - 1; h >= 0; --h) {
+        const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
+        const int mo = p->max_own[h], mf = p->max_f[h];
+        if (cnt <= 0 || mo <= 0) continue;
+        bnd<T, false>(D, node0, cnt, mo, mf, fronts, x, s);
+        const dim3 g((mo + VT - 1) / VT, cnt);
+        inv_gather_kernel<false><<<g, VT, 0, s>>>(D, node0, piv, x, scratch);
+        launched();
+        inv_apply_kernel<T, false><<<g, VT, sizeof(T) * mo, s>>>(D, node0, fronts, scratch, x);
+        launched();
+    }
+    return cuda_status();
+}
+
+}  // namespace nd
+}  // namespace tf
+
+using namespace tf;
+
+extern "C" size_t tf_nd_invert_workspace_bytes(const tf_nd_plan *plan, int elem_size) {
+    if (!plan || (elem_size != 4 && elem_size != 8)) return 0;
+    return nd::invert_work_elems(plan) * (size_t)elem_size;
+}
+
+extern "C" int tf_nd_invert_f64(const tf_nd_plan *plan, double *d_fronts, double *d_work, size_t work_bytes,
+                                tf_stream_t stream) {
+    int e = nd::check_plan(plan);
+    if (e) return e;
+    if (!d_fronts || (!d_work && nd::invert_work_elems(plan))) return TF_ERR_ARG;
+    return nd::invert<double>(plan, nd::dev_plan(plan, plan->d_rank), d_fronts, d_work, work_bytes,
+                              (cudaStream_t)stream);
+}
+
+extern "C" int tf_nd_invert_f32(const tf_nd_plan *plan, float *d_fronts, float *d_work, size_t work_bytes,
+                                tf_stream_t stream) {
+    int e = nd::check_plan(plan);
+    if (e) return e;
+    if (!d_fronts || (!d_work && nd::invert_work_elems(plan))) return TF_ERR_ARG;
+    return nd::invert<float>(plan, nd::dev_plan(plan, plan->d_rank), d_fronts, d_work, work_bytes,
+                             (cudaStream_t)stream);
+}
+
+extern "C" int tf_nd_solve_inv_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_t *d_piv,
+                                   double *d_x, double *d_scratch, tf_stream_t stream) {
+    int e = nd::check_plan(plan);
+    if (e) return e;
+    if (!d_fronts || !d_piv || !d_x || !d_scratch) return TF_ERR_ARG;
+    return nd::solve_inv<double>(plan, nd::dev_plan(plan, plan->d_rank), d_fronts, d_piv, d_x, d_scratch,
+                                 (cudaStream_t)stream);
+}
+
+extern "C" int tf_nd_solve_inv_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,
+                                   double *d_x, double *d_scratch, tf_stream_t stream) {
+    int e = nd::check_plan(plan);
+    if (e) return e;
+    if (!d_fronts || !d_piv || !d_x || !d_scratch) return TF_ERR_ARG;
+    return nd::solve_inv<float>(plan, nd::dev_plan(plan, plan->d_rank), d_fronts, d_piv, d_x, d_scratch,
+                                (cudaStream_t)stream);
+}

@@ -26,6 +26,9 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       after a failed attempt, grown after a success) and with
                       at most as many GMRES iterations as cost one
                       factorisation (both measured); 'always'
+  'Inverse Apply'     invert the factored own blocks once per factorisation
+                      and apply them by parallel triangular products instead
+                      of substitution (default True)
   'CUDA Graphs'       replay the factorisation and solve launch sequences from
                       captured CUDA graphs (default True)
   'Fuse Jacobian'     compute the Jacobian together with the RHS and reuse it
@@ -121,7 +124,8 @@ class Interface:
                              reuse_maxit=opts.get('Reuse Iterations', 20),
                              graphs=opts.get('CUDA Graphs', True),
                              reuse_policy=opts.get('Reuse Policy', 'cost'),
-                             reuse_drift=opts.get('Reuse Drift', 0.05))
+                             reuse_drift=opts.get('Reuse Drift', 0.05),
+                             inverse=opts.get('Inverse Apply', True))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

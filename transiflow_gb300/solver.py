@@ -213,17 +213,38 @@ class _Engine:
         self.vec = torch.empty(plan.host.n, dtype=torch.float64, device=solver.itf.device)
         fronts, piv = solver._fronts_raw(precision)
         info = solver.info
-        fac_fn = lib.tf_nd_factor_f64 if precision == 'fp64' else lib.tf_nd_factor_f32
-        sol_fn = lib.tf_nd_solve_f64 if precision == 'fp64' else lib.tf_nd_solve_f32
+        f64 = precision == 'fp64'
+        fac_fn = lib.tf_nd_factor_f64 if f64 else lib.tf_nd_factor_f32
         sp = _struct_ptr(plan.struct)
+        dev = solver.itf.device
+        if solver.inverse:
+            # invert the own blocks once per factorisation; apply with
+            # parallel triangular products instead of substitution chains
+            inv_fn = lib.tf_nd_invert_f64 if f64 else lib.tf_nd_invert_f32
+            sol_fn = lib.tf_nd_solve_inv_f64 if f64 else lib.tf_nd_solve_inv_f32
+            wbytes = lib.tf_nd_invert_workspace_bytes(sp, 8 if f64 else 4)
+            self.work = torch.empty(max(1, (wbytes + 7) // 8), dtype=torch.float64, device=dev)
+            self.scratch = torch.empty(plan.host.n, dtype=torch.float64, device=dev)
 
-        def factor():
-            _lib.check(fac_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(), info.data_ptr(),
-                              _stream()), 'tf_nd_factor')
+            def factor():
+                _lib.check(fac_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
+                                  info.data_ptr(), _stream()), 'tf_nd_factor')
+                _lib.check(inv_fn(sp, fronts.data_ptr(), self.work.data_ptr(), wbytes, _stream()),
+                           'tf_nd_invert')
 
-        def solve():
-            _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(), _stream()),
-                       'tf_nd_solve')
+            def solve():
+                _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(),
+                                  self.scratch.data_ptr(), _stream()), 'tf_nd_solve_inv')
+        else:
+            sol_fn = lib.tf_nd_solve_f64 if f64 else lib.tf_nd_solve_f32
+
+            def factor():
+                _lib.check(fac_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
+                                  info.data_ptr(), _stream()), 'tf_nd_factor')
+
+            def solve():
+                _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(), _stream()),
+                           'tf_nd_solve')
 
         if graphs:
             self.factor = _Graphed(factor, solver.stats)
@@ -241,8 +262,9 @@ class Solver:
     """Per-interface solver state: the plan, factor buffers, Krylov workspace."""
 
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
-                 reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05):
+                 reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True):
         self.itf = interface
+        self.inverse = inverse
         self.graphs = graphs
         self._engines = {}
         self.reuse = reuse
