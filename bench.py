@@ -219,7 +219,8 @@ def gpu_arm(args, rank, world, local):
               'roofline': roof, 'clocks': clk, 'gpu_launches': int(launches),
               'branch': {'points': calls.get('points'), 'rhs': calls.get('rhs'), 'jacobian': calls.get('jacobian'),
                          'solve': calls.get('solve'), 'factorizations': calls.get('factorizations'),
-                         'final_re': mu, 'final_fnorm': fnorm_end, 'per_step_solver': solver_stats}}
+                         'final_re': mu, 'final_fnorm': fnorm_end, 'per_step_solver': solver_stats,
+                         'newton_steps_per_s': (calls.get('jacobian') or 0) / t_step}}
     if rank == 0 and not args.no_baseline:
         result['cpu_baseline'] = cpu_baseline(args, calls)
     return result

@@ -276,7 +276,10 @@ int tf_nd_invert_f64(const tf_nd_plan *plan, double *d_fronts, double *d_work, s
 int tf_nd_invert_f32(const tf_nd_plan *plan, float *d_fronts, float *d_work, size_t work_bytes,
                      tf_stream_t stream);
 /* In-place solve with inverted own blocks (after tf_nd_invert_*): d_x as in
- * tf_nd_solve_*; d_scratch: plan->n doubles of device scratch.              */
+ * tf_nd_solve_*; d_scratch: tf_nd_solve_inv_workspace_bytes(plan) bytes of
+ * device scratch (one value per front index entry; the query reads the
+ * plan's last index offset from the device, a synchronising copy).         */
+size_t tf_nd_solve_inv_workspace_bytes(const tf_nd_plan *plan);
 int tf_nd_solve_inv_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_t *d_piv,
                         double *d_x, double *d_scratch, tf_stream_t stream);
 int tf_nd_solve_inv_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,

@@ -29,7 +29,7 @@ namespace tf {
 namespace nd {
 
 constexpr int IB = 32;        // diagonal block size
-constexpr int IT = 64;        // GEMM tile
+constexpr int IT = 32;        // GEMM tile (small: the top fronts' few splits must still fill the SMs)
 constexpr int IK = 32;        // GEMM k chunk
 constexpr int ITHREADS = 256;
 
@@ -130,8 +130,8 @@ __global__ void __launch_bounds__(ITHREADS) inv_gemm_kernel(DevPlan P, int node0
     }
     __shared__ T As[IK][IT + 1];   // As[k][i]
     __shared__ T Bs[IK][IT + 1];   // Bs[k][j]
-    const int tr = (threadIdx.x / 16) * 4, tc = (threadIdx.x % 16) * 4;
-    T acc[4][4] = {};
+    const int tr = (threadIdx.x / 16) * 2, tc = (threadIdx.x % 16) * 2;
+    T acc[2][2] = {};
     for (int k0 = klo - (klo % IK); k0 < khi; k0 += IK) {
         for (int t = threadIdx.x; t < IK * IT; t += ITHREADS) {
             const int kk = t % IK, ii = t / IK;   // A tile: consecutive threads along k
@@ -168,22 +168,22 @@ __global__ void __launch_bounds__(ITHREADS) inv_gemm_kernel(DevPlan P, int node0
         __syncthreads();
 #pragma unroll 8
         for (int kk = 0; kk < IK; ++kk) {
-            T a[4], b[4];
+            T a[2], b[2];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) { a[u] = As[kk][tr + u]; b[u] = Bs[kk][tc + u]; }
+            for (int u = 0; u < 2; ++u) { a[u] = As[kk][tr + u]; b[u] = Bs[kk][tc + u]; }
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < 2; ++u)
 #pragma unroll
-                for (int v = 0; v < 4; ++v) acc[u][v] += a[u] * b[v];
+                for (int v = 0; v < 2; ++v) acc[u][v] += a[u] * b[v];
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 2; ++u) {
         const int i = i0 + tr + u;
         if (i >= M) continue;
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
+        for (int v = 0; v < 2; ++v) {
             const int j = j0 + tc + v;
             if (j >= N) continue;
             if (STAGE == 0)
@@ -238,68 +238,103 @@ static int invert(const tf_nd_plan *p, const DevPlan &D, T *fronts, T *work, siz
 // ---------------------------------------------------------------------------
 // Application with the inverted blocks.
 // ---------------------------------------------------------------------------
-constexpr int VT = 128;   // rows per CTA of the triangular products
+constexpr int VT = 128;            // threads per CTA of the gather
+constexpr int VW = 8;              // rows (one warp each) per CTA of the products
 
-// scratch[g[c]] = x[g[pv[c]]] (forward, with the row permutation) or
-// x[g[c]] (backward) for the own rows of every front of one height.
+// packed[idx_off + c] = x[g[pv[c]]] (forward, with the row permutation) or
+// x[g[c]] (backward) for the own rows of every front of one height: each
+// front's right-hand side contiguous for the products below.
 template <bool FWD>
 __global__ void __launch_bounds__(VT) inv_gather_kernel(DevPlan P, int node0, const int32_t *piv, const double *x,
-                                                        double *scratch) {
+                                                        double *packed) {
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node];
     const int c = blockIdx.x * VT + threadIdx.x;
     if (c >= n) return;
     const int32_t *g = P.idx + P.idx_off[node];
-    scratch[g[c]] = FWD ? x[g[piv[P.piv_off[node] + c]]] : x[g[c]];
+    packed[P.idx_off[node] + c] = FWD ? x[g[piv[P.piv_off[node] + c]]] : x[g[c]];
 }
 
 // x[g[r]] = (L11^-1 s)_r (forward; unit diagonal) or (U11^-1 s)_r
-// (backward) for the own rows, s = scratch[g[.]] staged in shared memory;
-// one row per thread streaming through the L1 cache.
+// (backward) for the own rows: one warp per row, lanes over the columns
+// (coalesced reads of the row and of s), then a shuffle sum.  The shuffle
+// costs five FP64 adds per row against the row's length / 32 products per
+// lane; in exchange the large fronts near the root spread over many SMs.
 template <typename T, bool FWD>
-__global__ void __launch_bounds__(VT) inv_apply_kernel(DevPlan P, int node0, const T *fronts, const double *scratch,
-                                                       double *x) {
-    extern __shared__ unsigned char smem_raw[];
-    T *sv = reinterpret_cast<T *>(smem_raw);
+__global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0, const T *fronts,
+                                                            const double *packed, double *x) {
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
-    if (blockIdx.x * VT >= n) return;
-    const int32_t *g = P.idx + P.idx_off[node];
-    for (int c = threadIdx.x; c < n; c += VT) sv[c] = (T)scratch[g[c]];
-    __syncthreads();
-    const int r = blockIdx.x * VT + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * VW + (threadIdx.x >> 5);
     if (r >= n) return;
+    const double *sv = packed + P.idx_off[node];
     const T *row = fronts + P.front_off[node] + (size_t)r * f;
     const int c0 = FWD ? 0 : r, c1 = FWD ? r : n;
-    T s0 = FWD ? sv[r] : T(0), s1 = T(0), s2 = T(0), s3 = T(0);
-    int c = c0;
-    for (; c + 4 <= c1; c += 4) {
-        s0 += __ldg(row + c) * sv[c];
-        s1 += __ldg(row + c + 1) * sv[c + 1];
-        s2 += __ldg(row + c + 2) * sv[c + 2];
-        s3 += __ldg(row + c + 3) * sv[c + 3];
+    T s0 = T(0), s1 = T(0);
+    int c = c0 + lane;
+    for (; c + 32 < c1; c += 64) {
+        s0 += row[c] * (T)sv[c];
+        s1 += row[c + 32] * (T)sv[c + 32];
     }
-    for (; c < c1; ++c) s0 += __ldg(row + c) * sv[c];
-    x[g[r]] = (double)((s0 + s1) + (s2 + s3));
+    if (c < c1) s0 += row[c] * (T)sv[c];
+    T s = s0 + s1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        const int32_t *g = P.idx + P.idx_off[node];
+        x[g[r]] = FWD ? (double)s + sv[r] : (double)s;
+    }
+}
+
+// The same product with one row per thread, for FP64 heights whose own
+// blocks are short (the leaves): a warp's rows would be too short to pay for
+// its FP64 shuffle sum.  Threads of a warp read the same s[c] (a broadcast) and their
+// own rows through the L1 cache.
+constexpr int VS = 128;            // own rows up to which a thread takes a row
+
+template <typename T, bool FWD>
+__global__ void __launch_bounds__(VT) inv_apply_rows_kernel(DevPlan P, int node0, const T *fronts,
+                                                            const double *packed, double *x) {
+    const int node = node0 + blockIdx.y;
+    const int n = P.n_own[node], f = P.f[node];
+    const int r = blockIdx.x * VT + threadIdx.x;
+    if (r >= n) return;
+    const double *sv = packed + P.idx_off[node];
+    const T *row = fronts + P.front_off[node] + (size_t)r * f;
+    const int c0 = FWD ? 0 : r, c1 = FWD ? r : n;
+    T s0 = T(0), s1 = T(0);
+    int c = c0;
+    for (; c + 2 <= c1; c += 2) {
+        s0 += row[c] * (T)sv[c];
+        s1 += row[c + 1] * (T)sv[c + 1];
+    }
+    if (c < c1) s0 += row[c] * (T)sv[c];
+    const int32_t *g = P.idx + P.idx_off[node];
+    x[g[r]] = FWD ? (double)(s0 + s1) + sv[r] : (double)(s0 + s1);
+}
+
+template <typename T, bool FWD>
+static void inv_apply(const DevPlan &D, int node0, int cnt, int mo, const T *fronts, const double *packed, double *x,
+                      cudaStream_t s) {
+    // FP32 shuffles are cheap, so single precision always takes a warp per row
+    if (sizeof(T) == 8 && mo <= VS)
+        inv_apply_rows_kernel<T, FWD><<<dim3((mo + VT - 1) / VT, cnt), VT, 0, s>>>(D, node0, fronts, packed, x);
+    else
+        inv_apply_kernel<T, FWD><<<dim3((mo + VW - 1) / VW, cnt), 32 * VW, 0, s>>>(D, node0, fronts, packed, x);
+    launched();
 }
 
 template <typename T>
 static int solve_inv(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int32_t *piv, double *x,
-                     double *scratch, cudaStream_t s) {
-    size_t mo_all = 0;
-    for (int h = 0; h < p->nlevels; ++h) mo_all = std::max(mo_all, (size_t)p->max_own[h]);
-    int e = ensure_smem((const void *)inv_apply_kernel<T, true>, sizeof(T) * mo_all);
-    if (!e) e = ensure_smem((const void *)inv_apply_kernel<T, false>, sizeof(T) * mo_all);
-    if (e) return e;
+                     double *packed, cudaStream_t s) {
     for (int h = 0; h < p->nlevels; ++h) {
         const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
         const int mo = p->max_own[h], mf = p->max_f[h];
         if (cnt <= 0 || mo <= 0) continue;
-        const dim3 g((mo + VT - 1) / VT, cnt);
-        inv_gather_kernel<true><<<g, VT, 0, s>>>(D, node0, piv, x, scratch);
+        inv_gather_kernel<true><<<dim3((mo + VT - 1) / VT, cnt), VT, 0, s>>>(D, node0, piv, x, packed);
         launched();
-        inv_apply_kernel<T, true><<<g, VT, sizeof(T) * mo, s>>>(D, node0, fronts, scratch, x);
-        launched();
+        inv_apply<T, true>(D, node0, cnt, mo, fronts, packed, x, s);
         bnd<T, true>(D, node0, cnt, mf, mo, fronts, x, s);
     }
     for (int h = p->nlevels - 1; h >= 0; --h) {
@@ -307,11 +342,9 @@ static int solve_inv(const tf_nd_plan *p, const DevPlan &D, const T *fronts, con
         const int mo = p->max_own[h], mf = p->max_f[h];
         if (cnt <= 0 || mo <= 0) continue;
         bnd<T, false>(D, node0, cnt, mo, mf, fronts, x, s);
-        const dim3 g((mo + VT - 1) / VT, cnt);
-        inv_gather_kernel<false><<<g, VT, 0, s>>>(D, node0, piv, x, scratch);
+        inv_gather_kernel<false><<<dim3((mo + VT - 1) / VT, cnt), VT, 0, s>>>(D, node0, piv, x, packed);
         launched();
-        inv_apply_kernel<T, false><<<g, VT, sizeof(T) * mo, s>>>(D, node0, fronts, scratch, x);
-        launched();
+        inv_apply<T, false>(D, node0, cnt, mo, fronts, packed, x, s);
     }
     return cuda_status();
 }
@@ -324,6 +357,16 @@ using namespace tf;
 extern "C" size_t tf_nd_invert_workspace_bytes(const tf_nd_plan *plan, int elem_size) {
     if (!plan || (elem_size != 4 && elem_size != 8)) return 0;
     return nd::invert_work_elems(plan) * (size_t)elem_size;
+}
+
+extern "C" size_t tf_nd_solve_inv_workspace_bytes(const tf_nd_plan *plan) {
+    if (nd::check_plan(plan)) return 0;
+    int64_t len = 0;
+    if (cudaMemcpy(&len, plan->d_idx_off + plan->nnodes, sizeof(len), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return (size_t)len * sizeof(double);
 }
 
 extern "C" int tf_nd_invert_f64(const tf_nd_plan *plan, double *d_fronts, double *d_work, size_t work_bytes,

@@ -224,7 +224,8 @@ class _Engine:
             sol_fn = lib.tf_nd_solve_inv_f64 if f64 else lib.tf_nd_solve_inv_f32
             wbytes = lib.tf_nd_invert_workspace_bytes(sp, 8 if f64 else 4)
             self.work = torch.empty(max(1, (wbytes + 7) // 8), dtype=torch.float64, device=dev)
-            self.scratch = torch.empty(plan.host.n, dtype=torch.float64, device=dev)
+            sbytes = lib.tf_nd_solve_inv_workspace_bytes(sp)
+            self.scratch = torch.empty(max(1, sbytes // 8), dtype=torch.float64, device=dev)
 
             def factor():
                 _lib.check(fac_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
@@ -246,6 +247,7 @@ class _Engine:
                 _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(), _stream()),
                            'tf_nd_solve')
 
+        self.solve_raw = solve
         if graphs:
             self.factor = _Graphed(factor, solver.stats)
             self.solve = _Graphed(solve, solver.stats)
@@ -279,6 +281,9 @@ class Solver:
         # adapted: halved after a failed attempt, grown after a success
         self._drift_tol = reuse_drift
         self._drift_work = None
+        self._steps = {}
+        self._opbuf = None
+        self._opbuf_src = None
         # solves per operator and GMRES iterations with a fresh factorisation
         self._solves_per_op = 1.0
         self._its_fresh = 1.0
@@ -369,6 +374,7 @@ class Solver:
     def _workspace(self, n, dev):
         m = self.restart
         if self._V is None or self._V.shape[1] != n:
+            self._steps = {}
             self._V = torch.empty((m + 1, n), dtype=torch.float64, device=dev)
             self._Z = torch.empty((m, n), dtype=torch.float64, device=dev)
             lib = _lib.load()
@@ -414,6 +420,49 @@ class Solver:
         out = self._mdot(w.view(1, -1), 1, w)
         return math.sqrt(max(float(out.item()), 0.0))
 
+    def _arnoldi_step(self, op, fac, j):
+        """One flexible Arnoldi step on fixed buffers: Z[j] = M^-1 V[j],
+        w = A Z[j] into V[j+1], classical Gram-Schmidt twice against V[0..j]
+        (coefficients into the host-read buffer), ||w||^2 last, w scaled to
+        unit norm.  The operator's values sit in a fixed buffer too, so every
+        (precision, j) step is one CUDA graph, captured on its second use and
+        replayed afterwards."""
+        if self._opbuf is None or self._opbuf.numel() != op.values.numel():
+            self._opbuf = torch.empty_like(op.values)
+            self._opbuf_src = None
+        if self._opbuf_src is not op:
+            self._copy(op.values, self._opbuf)
+            self._opbuf_src = op
+        key = (fac.precision, j)
+        step = self._steps.get(key)
+        if step is None:
+            eng = self._engine(fac.precision)
+            V, Z = self._V, self._Z
+            hbuf = self._hbuf[:2 * (j + 1) + 1]
+            h, h2, ww = hbuf[:j + 1], hbuf[j + 1:2 * (j + 1)], hbuf[2 * (j + 1):]
+            w = V[j + 1]
+            lib = _lib.load()
+            pat = op.jac.pattern
+            opbuf = self._opbuf
+
+            def fn():
+                self._copy(V[j], eng.vec)
+                eng.solve_raw()
+                self._copy(eng.vec, Z[j])
+                _lib.check(lib.tf_spmv_f64(op.n, pat.rowptr.data_ptr(), pat.cols.data_ptr(), opbuf.data_ptr(),
+                                           Z[j].data_ptr(), w.data_ptr(), 1.0, 0.0, _stream()), 'tf_spmv_f64')
+                self._mdot_into(V, j + 1, w, h)
+                self._mgs(V, j + 1, h, w)
+                self._mdot_into(V, j + 1, w, h2)
+                self._mgs(V, j + 1, h2, w)
+                self._mdot_into(w.view(1, -1), 1, w, ww)
+                # a zero norm (breakdown) makes w non-finite; the caller stops there
+                torch.mul(w, torch.rsqrt(ww), out=w)
+
+            step = _Graphed(fn, self.stats) if self.graphs else fn
+            self._steps[key] = step
+        step()
+
     def fgmres(self, op, fac, b, maxit=None):
         """Solve A_g x = b (b: float64 CUDA tensor) with preconditioner fac;
         returns (x, iterations, relres)."""
@@ -448,25 +497,13 @@ class Solver:
             sn = np.zeros(m)
             k = 0
             for j in range(m):
-                self._copy(V[j], Z[j])
-                fac.apply(Z[j])
-                op.matvec(Z[j], V[j + 1])
-                w = V[j + 1]
-                # CGS2 and the new vector's norm, read back with one sync
-                hbuf = self._hbuf[:2 * (j + 1) + 1]
-                h, h2, ww = hbuf[:j + 1], hbuf[j + 1:2 * (j + 1)], hbuf[2 * (j + 1):]
-                self._mdot_into(V, j + 1, w, h)
-                self._mgs(V, j + 1, h, w)
-                self._mdot_into(V, j + 1, w, h2)
-                self._mgs(V, j + 1, h2, w)
-                self._mdot_into(w.view(1, -1), 1, w, ww)
-                hb = hbuf.cpu().numpy()
+                self._arnoldi_step(op, fac, j)
+                # the CGS2 coefficients and the new vector's norm, one sync
+                hb = self._hbuf[:2 * (j + 1) + 1].cpu().numpy()
                 hh = hb[:j + 1] + hb[j + 1:2 * (j + 1)]
                 hn = math.sqrt(max(float(hb[-1]), 0.0))
                 H[:j + 1, j] = hh
                 H[j + 1, j] = hn
-                if hn > 0:
-                    self._axpby(1.0 / hn, w, 0.0, None, w)
                 for i in range(j):
                     t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
                     H[i + 1, j] = -sn[i] * H[i, j] + cs[i] * H[i + 1, j]
