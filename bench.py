@@ -62,6 +62,8 @@ def parse():
                     help='time this many random lid-driven cavities (nx from 32..192, Re from [100, 4000], '
                          'seed 2) solved concurrently and one after the other, then exit')
     ap.add_argument('--re', type=float, default=1000.0, help='Reynolds number of the --profile state')
+    ap.add_argument('--apply', default='levels', choices=['flow', 'levels'],
+                    help='application of the inverted factors: one dataflow launch or one launch per tree height')
     return ap.parse_args()
 
 
@@ -151,7 +153,8 @@ def gpu_arm(args, rank, world, local):
     from transiflow_gb300 import Continuation, Interface, _lib, dist
     torch.cuda.set_device(local)
     lib = _lib.load()
-    params = {'CUDA': {'Factor Precision': args.precision, 'Tolerance': args.tol}}
+    params = {'CUDA': {'Factor Precision': args.precision, 'Tolerance': args.tol,
+                       'Dataflow Apply': args.apply == 'flow'}}
     itf = Interface(params, args.nx, args.nx, args.nz)
     n = itf.n
     stream = torch.cuda.current_stream()
@@ -431,7 +434,8 @@ def profile_stage(args):
     each timed with CUDA events on the launching stream."""
     import torch
     from transiflow_gb300 import Interface
-    p = {'Reynolds Number': args.re, 'CUDA': {'Factor Precision': args.precision, 'CUDA Graphs': False}}
+    p = {'Reynolds Number': args.re, 'CUDA': {'Factor Precision': args.precision, 'CUDA Graphs': False,
+                                              'Dataflow Apply': args.apply == 'flow'}}
     itf = Interface(p, args.nx, args.nx, args.nz)
     s = 0.1 * np.random.default_rng(1).standard_normal(itf.n)
     x = itf.vector_from_array(s)

@@ -48,7 +48,8 @@ enum {
     TF_ERR_ARG = 1,          /* invalid argument (null pointer, bad size)   */
     TF_ERR_UNSUPPORTED = 2,  /* (dim, dof) combination not compiled in      */
     TF_ERR_CUDA = 3,         /* a CUDA launch or runtime call failed        */
-    TF_ERR_SIZE = 4          /* a size exceeds a compiled-in maximum        */
+    TF_ERR_SIZE = 4,         /* a size exceeds a compiled-in maximum        */
+    TF_ERR_TIMEOUT = 5       /* a bounded device-side wait gave up          */
 };
 
 /* ---- problem description -------------------------------------------------*/
@@ -284,6 +285,29 @@ int tf_nd_solve_inv_f64(const tf_nd_plan *plan, const double *d_fronts, const in
                         double *d_x, double *d_scratch, tf_stream_t stream);
 int tf_nd_solve_inv_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,
                         double *d_x, double *d_scratch, tf_stream_t stream);
+
+/* The same application as tf_nd_solve_inv_* in ONE persistent launch: both
+ * sweeps run as a task list over the elimination tree, each task waiting
+ * (bounded) only for the fronts it depends on.  Setup, once per plan:
+ * tf_nd_flow_workspace_bytes (0 on a bad plan) and tf_nd_flow_prepare, both
+ * synchronising (they read the plan's front sizes from the device).
+ * elem_size: 8 (f64 fronts) or 4 (f32); TF_ERR_SIZE when the plan's widest
+ * front does not fit the launch's shared memory (use tf_nd_solve_inv_*).
+ * fuse_tiles: fronts with at most this many 32x32 factor tiles per sweep run
+ * as one task (0: never); chunk_tiles: target tiles per task of the others.
+ * d_work is then passed to every solve (one application at a time per
+ * workspace).  tf_nd_flow_status returns and clears the sticky error word:
+ * TF_ERR_TIMEOUT when a wait gave up (the solution is then invalid), a
+ * synchronising read.  No counterpart in the reference (SciPy.py:194-202
+ * substitutes with SuperLU's factors).                                       */
+size_t tf_nd_flow_workspace_bytes(const tf_nd_plan *plan, int fuse_tiles, int chunk_tiles);
+int tf_nd_flow_prepare(const tf_nd_plan *plan, void *d_work, size_t work_bytes, int elem_size,
+                       int fuse_tiles, int chunk_tiles);
+int tf_nd_solve_flow_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_t *d_piv,
+                         double *d_x, void *d_work, tf_stream_t stream);
+int tf_nd_solve_flow_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,
+                         double *d_x, void *d_work, tf_stream_t stream);
+int tf_nd_flow_status(void *d_work);
 
 #ifdef __cplusplus
 }

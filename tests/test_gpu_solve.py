@@ -107,3 +107,54 @@ def test_one_application_of_the_inverted_factors_solves(shape, params):
     ref = spla.spsolve(A.tocsc(), out['b'])
     assert np.linalg.norm(out[True] - ref) <= 1e-9 * np.linalg.norm(ref)
     assert np.linalg.norm(out[True] - out[False]) <= 1e-9 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'fp32'])
+@pytest.mark.parametrize('shape,params', [((40, 36, 1), {'Reynolds Number': 1500}),
+                                          ((7, 6, 6), {'Reynolds Number': 200}),
+                                          ((12, 10, 1), {'Problem Type': 'Rayleigh-Benard',
+                                                         'Rayleigh Number': 1800, 'Prandtl Number': 10}),
+                                          ((16, 8, 1), {'Problem Type': 'AMOC', 'Rayleigh Number': 4e4,
+                                                        'Prandtl Number': 2.25, 'X-max': 5,
+                                                        'Temperature Forcing': 1.0})])
+def test_dataflow_application_matches_per_height_launches(shape, params, precision):
+    """The one-launch dataflow application of the inverted factors gives the
+    per-height application's result (up to the order of the sums) for every
+    split of the fronts into tasks: all split into single strips, the
+    defaults, all fused; and its bounded waits report no time-out."""
+    import torch
+    from transiflow_gb300 import Interface
+    nx, ny, nz = shape
+    b = None
+    results = {}
+    for flow, fuse, chunk in [(False, 48, 24), (True, 0, 1), (True, 0, 24), (True, 48, 24), (True, 10 ** 6, 24)]:
+        p = dict(params)
+        p['CUDA'] = {'Factor Precision': precision, 'CUDA Graphs': False, 'Dataflow Apply': flow,
+                     'Dataflow Fuse Tiles': fuse, 'Dataflow Chunk Tiles': chunk}
+        itf = Interface(p, nx, ny, nz)
+        st = 0.3 * np.random.default_rng(4).standard_normal(itf.n)
+        J = itf.jacobian(itf.vector_from_array(st))
+        fac = itf.solver.factorization(J)
+        eng = itf.solver._engine(precision)
+        assert (eng.flow is not None) == flow
+        if b is None:
+            b = np.random.default_rng(5).standard_normal(itf.n)
+            b[itf.dim] = 0.0
+        v = torch.as_tensor(b.copy()).to(itf.device)
+        fac.apply(v)
+        fac.apply(v)      # a second application reuses the cleared counters
+        eng.check()
+        results[(flow, fuse, chunk)] = v.cpu().numpy()
+    base = results.pop((False, 48, 24))
+    if precision == 'fp64':
+        for key, r in results.items():
+            assert np.all(np.isfinite(r)), key
+            assert np.linalg.norm(r - base) <= 1e-11 * np.linalg.norm(base), key
+    else:
+        # single-precision factors: both orders of summation are equally
+        # accurate against the FP64 sparse direct solution
+        ref = spla.spsolve(_gauged(J.to_scipy(), itf.dim).tocsc(), b)
+        err_base = np.linalg.norm(base - ref) / np.linalg.norm(ref)
+        for key, r in results.items():
+            assert np.all(np.isfinite(r)), key
+            assert np.linalg.norm(r - ref) / np.linalg.norm(ref) <= 3 * err_base + 1e-6, key

@@ -796,6 +796,7 @@ extern "C" const char *tf_error_string(int code) {
         case TF_ERR_UNSUPPORTED: return "unsupported (dim, dof) combination";
         case TF_ERR_CUDA: return "CUDA error";
         case TF_ERR_SIZE: return "size exceeds a compiled-in limit";
+        case TF_ERR_TIMEOUT: return "a device-side wait gave up";
         default: return "unknown error";
     }
 }

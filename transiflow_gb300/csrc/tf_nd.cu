@@ -146,6 +146,56 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(DevPlan P, int node0, int
     }
 }
 
+// FP32 trailing update with 128 x 128 tiles, 8 x 8 outputs per thread: the
+// FP32 pipe is 64 times the FP64 one, so in single precision the update is
+// bound by the tile's memory traffic and wants the larger tile (used for
+// the large fronts; the 64 x 64 kernel above covers small ones and FP64).
+constexpr int TB = 128;
+
+__global__ void __launch_bounds__(THREADS) gemm128_kernel(DevPlan P, int node0, int k, float *fronts) {
+    const int node = node0 + blockIdx.z;
+    const int n = P.n_own[node], f = P.f[node];
+    if (k >= n) return;
+    const int nb = min(NB, n - k);
+    const int r0 = k + nb + blockIdx.y * TB, c0 = k + nb + blockIdx.x * TB;
+    if (r0 >= f || c0 >= f) return;
+    float *F = fronts + P.front_off[node];
+    __shared__ float As[NB][TB + 4];   // As[q][r]
+    __shared__ float Bs[NB][TB + 4];   // Bs[q][c]
+    for (int t = threadIdx.x; t < NB * TB; t += THREADS) {
+        const int q = t % NB, r = t / NB;
+        As[q][r] = (q < nb && r0 + r < f) ? F[(size_t)(r0 + r) * f + k + q] : 0.f;
+    }
+    for (int t = threadIdx.x; t < NB * TB; t += THREADS) {
+        const int q = t / TB, c = t % TB;
+        Bs[q][c] = (q < nb && c0 + c < f) ? F[(size_t)(k + q) * f + c0 + c] : 0.f;
+    }
+    __syncthreads();
+    const int tr = (threadIdx.x / 16) * 8, tc = (threadIdx.x % 16) * 8;
+    float acc[8][8] = {};
+#pragma unroll 4
+    for (int q = 0; q < NB; ++q) {
+        float a[8], b[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) { a[u] = As[q][tr + u]; b[u] = Bs[q][tc + u]; }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+#pragma unroll
+            for (int v = 0; v < 8; ++v) acc[u][v] += a[u] * b[v];
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        const int r = r0 + tr + u;
+        if (r >= f) continue;
+        float *row = F + (size_t)r * f;
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+            const int c = c0 + tc + v;
+            if (c < f) row[c] -= acc[u][v];
+        }
+    }
+}
+
 // Scatter the (gauged) stencil-CSR values into the fronts.
 template <typename T>
 __global__ void scatter_kernel(int64_t m, const int64_t *__restrict__ pos, const int32_t *__restrict__ src,
@@ -213,9 +263,6 @@ __global__ void __launch_bounds__(256) pivots_to_permutation_kernel(DevPlan P, i
 // rules out TMA) and every lane forms the dot product of one row serially.
 // The copies are issued ahead of the barrier or the tile before, so their
 // latency overlaps other work.
-constexpr int SB = 32;
-constexpr int TSTRIDE = SB + 1;
-constexpr int TILE = SB * TSTRIDE;      // elements of one padded 32 x 32 tile
 constexpr int TRI_WARPS = 4;
 constexpr int TRI_THREADS = 32 * TRI_WARPS;
 constexpr int GEMV_WARPS = 2;
@@ -223,44 +270,6 @@ constexpr int GEMV_THREADS = 32 * GEMV_WARPS;
 constexpr int GEMV_ROWS = 32 * GEMV_WARPS;
 constexpr int GEMV_TILES = 4;           // column tiles per warp
 constexpr int GEMV_COLS = GEMV_TILES * SB;
-
-template <typename T>
-__device__ __forceinline__ void cp_async_elem(T *dst, const T *src, bool valid) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    if (sizeof(T) == 8)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 8 : 0)
-                     : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 4 : 0)
-                     : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-// One warp: start copying the tile F[r0 .. r0+31][c0 .. c0+31] into buf
-// (row-major, stride TSTRIDE) and commit it as one group; entries with row
-// >= rmax or column >= cmax become zero.
-template <typename T>
-__device__ __forceinline__ void tile_issue(T *buf, const T *F, int f, int r0, int rmax, int c0, int cmax, int lane) {
-    const bool colok = c0 + lane < cmax;
-#pragma unroll 8
-    for (int i = 0; i < SB; ++i) {
-        const int r = r0 + i;
-        const bool ok = colok && r < rmax;
-        cp_async_elem(buf + i * TSTRIDE + lane, ok ? F + (size_t)r * f + c0 + lane : F, ok);
-    }
-    cp_async_commit();
-}
-
-// Lane l: sum_c buf[l][c] v[c].
-template <typename T>
-__device__ __forceinline__ T tile_dot(const T *buf, const T *v, int lane) {
-    T s = T(0);
-#pragma unroll 8
-    for (int c = 0; c < SB; ++c) s += buf[lane * TSTRIDE + c] * v[c];
-    return s;
-}
 
 // Triangular solves with the own block L11 (forward, unit lower, after the
 // row permutation) or U11 (backward) of every front of one height.  A front's
@@ -507,6 +516,14 @@ static int factor(const tf_nd_plan *p, const double *vals, T *fronts, int32_t *p
                 urow_kernel<T><<<gl, TRSM_THREADS, 0, s>>>(D, node0, k, fronts); launched();
             }
             if (rest > 0) {
+                if constexpr (sizeof(T) == 4) {
+                    if (rest >= 2 * TB) {
+                        const int tiles = (rest + TB - 1) / TB;
+                        gemm128_kernel<<<dim3(tiles, tiles, cnt), THREADS, 0, s>>>(D, node0, k, (float *)fronts);
+                        launched();
+                        continue;
+                    }
+                }
                 const int tiles = (rest + TM - 1) / TM;
                 dim3 gg(tiles, tiles, cnt);
                 gemm_kernel<T><<<gg, THREADS, 0, s>>>(D, node0, k, fronts); launched();

@@ -26,6 +26,50 @@ struct DevPlan {
 template <typename T>
 __device__ __forceinline__ T tabs(T x) { return x < T(0) ? -x : x; }
 
+// 32 x 32 tiles of a front staged in shared memory by cp.async (8- or
+// 4-byte copies: rows of a front start at arbitrary alignment).
+constexpr int SB = 32;
+constexpr int TSTRIDE = SB + 1;
+constexpr int TILE = SB * TSTRIDE;      // elements of one padded 32 x 32 tile
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *dst, const T *src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if (sizeof(T) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 8 : 0)
+                     : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 4 : 0)
+                     : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// One warp: start copying the tile F[r0 .. r0+31][c0 .. c0+31] into buf
+// (row-major, stride TSTRIDE) and commit it as one group; entries with row
+// >= rmax or column >= cmax become zero.
+template <typename T>
+__device__ __forceinline__ void tile_issue(T *buf, const T *F, int f, int r0, int rmax, int c0, int cmax, int lane) {
+    const bool colok = c0 + lane < cmax;
+#pragma unroll 8
+    for (int i = 0; i < SB; ++i) {
+        const int r = r0 + i;
+        const bool ok = colok && r < rmax;
+        cp_async_elem(buf + i * TSTRIDE + lane, ok ? F + (size_t)r * f + c0 + lane : F, ok);
+    }
+    cp_async_commit();
+}
+
+// Lane l: sum_c buf[l][c] v[c].
+template <typename T>
+__device__ __forceinline__ T tile_dot(const T *buf, const T *v, int lane) {
+    T s = T(0);
+#pragma unroll 8
+    for (int c = 0; c < SB; ++c) s += buf[lane * TSTRIDE + c] * v[c];
+    return s;
+}
+
 // Opts a kernel in to `bytes` of dynamic shared memory on the current device
 // (TF_ERR_SIZE when static plus dynamic shared memory would not fit).
 int ensure_smem(const void *kernel, size_t bytes);

@@ -236,6 +236,23 @@ __device__ __forceinline__ bool mbar_wait(void *bar, unsigned parity) {
     return false;
 }
 
+// Pivot-search key of an entry: the IEEE-754 bit pattern of |v| (non-negative
+// floating-point values order like their bit patterns), with NaN mapped to 0,
+// so that the searches compare on the integer pipe and leave the scarce FP64
+// pipe to the eliminations.  Rows that may not be chosen get key -1.
+__device__ __forceinline__ long long mag_key(double v) {
+    const long long b = __double_as_longlong(v) & 0x7fffffffffffffffll;
+    return b > 0x7ff0000000000000ll ? 0 : b;
+}
+__device__ __forceinline__ long long mag_key(float v) {
+    const int b = __float_as_int(v) & 0x7fffffff;
+    return b > 0x7f800000 ? 0 : b;
+}
+__device__ __forceinline__ void st_async(unsigned raddr, long long v, unsigned rbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];\n"
+                 ::"r"(raddr), "l"(v), "r"(rbar) : "memory");
+}
+
 // Row swaps of a finished panel applied to this CTA's share [c0, c1) of the
 // columns outside the panel (column j maps to j < k ? j : j + nb).  The
 // swap sequence (row lc <-> row piv[lc], in order) only moves rows among
@@ -252,6 +269,7 @@ __device__ void apply_panel_swaps(T *F, int f, int k, int nb, int c0, int c1, co
     __shared__ int sl[2 * NB];     // touched rows (relative to k)
     __shared__ int pc[NB];         // compact slot of s_piv[t]
     __shared__ int srcc[2 * NB];   // slot whose old content ends in slot c
+    __shared__ int cur[2 * NB];    // composition scratch (shared: indexed at run time)
     __shared__ int nsl;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (warp == 0) {
@@ -267,7 +285,6 @@ __device__ void apply_panel_swaps(T *F, int f, int k, int nb, int c0, int c1, co
         if (lane == 0) nsl = nb + __popc(ball);
         __syncwarp();
         if (lane == 0) {
-            int cur[2 * NB];
             const int m = nsl;
             for (int c = 0; c < m; ++c) cur[c] = c;
             for (int t = 0; t < nb; ++t) {
@@ -329,10 +346,10 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
     T *F = fronts + P.front_off[node];
     int32_t *pv = piv + P.piv_off[node];
     __shared__ T wrow[NW][NB];
-    __shared__ T wval[NW];
+    __shared__ long long wval[NW];
     __shared__ int widx[NW];
     __shared__ T lstage[NB];
-    __shared__ T cval[2][CL];
+    __shared__ long long cval[2][CL];   // candidates' pivot-search keys
     __shared__ T crcp[2][CL];      // 1 / (candidate's entry in column lc)
     __shared__ int cidx[2][CL];
     __shared__ T crow[2][CL][NB];
@@ -341,7 +358,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
     __shared__ __align__(8) unsigned long long mbar[2];
     // bytes each CTA receives per column: every CTA's candidate (row, value,
     // index, reciprocal pivot) and the diagonal row
-    constexpr unsigned TX = CL * (NB * sizeof(T) + 2 * sizeof(T) + sizeof(int)) + NB * sizeof(T);
+    constexpr unsigned TX = CL * (NB * sizeof(T) + sizeof(T) + sizeof(long long) + sizeof(int)) + NB * sizeof(T);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int my = lo + threadIdx.x;
     const bool have = my < hi;
@@ -362,11 +379,11 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
         if (lc < nb) {
             const int par = lc & 1;
             const int ql = lc / R;
-            T best = (have && my >= lc) ? tabs(a[lc]) : T(-1);
+            long long best = (have && my >= lc) ? mag_key(a[lc]) : -1ll;
             int bi = (have && my >= lc) ? my : 0x7fffffff;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                const T ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
                 const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
@@ -382,7 +399,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
             if (threadIdx.x == 0) mbar_expect_tx(&mbar[par], TX);
             __syncthreads();
             if (warp == 0) {
-                T b = wval[0];
+                long long b = wval[0];
                 int i = widx[0], ws = 0;
                 for (int w = 1; w < NW; ++w)
                     if (wval[w] > b || (wval[w] == b && widx[w] < i)) { b = wval[w]; i = widx[w]; ws = w; }
@@ -405,16 +422,16 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
             }
             if (!mbar_wait(&mbar[par], (lc >> 1) & 1) && threadIdx.x == 0 && info)
                 atomicAdd(info, 1 << 20);   // gave up waiting: reported as a failed factorisation
-            T b = T(-1);
+            long long b = -1;
             int r = 0x7fffffff, w = 0;
 #pragma unroll
             for (int c = 0; c < CL; ++c)
                 if (cval[par][c] > b || (cval[par][c] == b && cidx[par][c] < r)) { b = cval[par][c]; r = cidx[par][c]; w = c; }
             const T *prow = crow[par][w];
             T rp = crcp[par][w];
-            if (r >= rows) {   // no comparable candidate (NaN column)
+            if (r >= rows) {   // no candidate row (cannot happen while lc < rows)
                 r = lc;
-                b = T(0);
+                b = 0;
                 prow = lrow[par];
                 rp = T(1) / prow[lc];
             }
@@ -422,7 +439,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(PT)
                 s_piv[lc] = r;
                 if (q == 0) {
                     pv[k + lc] = k + r;
-                    if (b == T(0) && info) atomicAdd(info, 1);
+                    if (b == 0 && info) atomicAdd(info, 1);   // zero (or NaN) pivot
                 }
             }
             if (have) {
@@ -495,6 +512,10 @@ constexpr int PANEL_PT = 256;
 template <typename T, int CL>
 static int launch_panel_reg_pt(const DevPlan &D, int node0, int cnt, int k, int rows, T *fronts, int32_t *piv,
                                int32_t *info, cudaStream_t s) {
+    // the many small fronts near the leaves: 128-thread CTAs, twice as many
+    // resident per SM to hide the per-column latency
+    if constexpr (CL == 1)
+        if (rows <= PANEL_PT / 2) return launch_panel_reg<T, 1, PANEL_PT / 2>(D, node0, cnt, k, fronts, piv, info, s);
     if ((rows + CL - 1) / CL <= PANEL_PT) return launch_panel_reg<T, CL, PANEL_PT>(D, node0, cnt, k, fronts, piv, info, s);
     return TF_ERR_SIZE;
 }

@@ -29,6 +29,15 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
   'Inverse Apply'     invert the factored own blocks once per factorisation
                       and apply them by parallel triangular products instead
                       of substitution (default True)
+  'Dataflow Apply'    with 'Inverse Apply': run both sweeps of an application
+                      in one persistent launch in which each front waits only
+                      for the fronts it depends on (default False; plans whose
+                      widest front does not fit that launch's shared memory
+                      keep one launch per tree height)
+  'Dataflow Fuse Tiles', 'Dataflow Chunk Tiles'
+                      fronts with at most this many 32x32 factor tiles per
+                      sweep run as one task (default 48); target tiles per task
+                      of the other fronts (default 24)
   'CUDA Graphs'       replay the factorisation and solve launch sequences from
                       captured CUDA graphs (default True)
   'Fuse Jacobian'     compute the Jacobian together with the RHS and reuse it
@@ -125,7 +134,10 @@ class Interface:
                              graphs=opts.get('CUDA Graphs', True),
                              reuse_policy=opts.get('Reuse Policy', 'cost'),
                              reuse_drift=opts.get('Reuse Drift', 0.05),
-                             inverse=opts.get('Inverse Apply', True))
+                             inverse=opts.get('Inverse Apply', True),
+                             flow=opts.get('Dataflow Apply', False),
+                             flow_fuse_tiles=int(opts.get('Dataflow Fuse Tiles', 48)),
+                             flow_chunk_tiles=int(opts.get('Dataflow Chunk Tiles', 24)))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

@@ -224,19 +224,41 @@ class _Engine:
             sol_fn = lib.tf_nd_solve_inv_f64 if f64 else lib.tf_nd_solve_inv_f32
             wbytes = lib.tf_nd_invert_workspace_bytes(sp, 8 if f64 else 4)
             self.work = torch.empty(max(1, (wbytes + 7) // 8), dtype=torch.float64, device=dev)
-            sbytes = lib.tf_nd_solve_inv_workspace_bytes(sp)
-            self.scratch = torch.empty(max(1, sbytes // 8), dtype=torch.float64, device=dev)
+            self.flow = None
+            if solver.flow:
+                # both sweeps in one persistent launch (dataflow over the
+                # elimination tree); plans whose widest front does not fit
+                # the launch's shared memory keep the per-height launches
+                fuse, chunk = solver.flow_fuse_tiles, solver.flow_chunk_tiles
+                fbytes = lib.tf_nd_flow_workspace_bytes(sp, fuse, chunk)
+                if fbytes:
+                    flow = torch.empty((fbytes + 7) // 8, dtype=torch.float64, device=dev)
+                    code = lib.tf_nd_flow_prepare(sp, flow.data_ptr(), fbytes, 8 if f64 else 4, fuse, chunk)
+                    if code == 0:
+                        self.flow = flow
+                    elif code != 4:     # TF_ERR_SIZE: fall back to the per-height launches
+                        _lib.check(code, 'tf_nd_flow_prepare')
+            if self.flow is not None:
+                flow_fn = lib.tf_nd_solve_flow_f64 if f64 else lib.tf_nd_solve_flow_f32
+
+                def solve():
+                    _lib.check(flow_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(),
+                                       self.flow.data_ptr(), _stream()), 'tf_nd_solve_flow')
+            else:
+                sbytes = lib.tf_nd_solve_inv_workspace_bytes(sp)
+                self.scratch = torch.empty(max(1, sbytes // 8), dtype=torch.float64, device=dev)
+
+                def solve():
+                    _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(),
+                                      self.scratch.data_ptr(), _stream()), 'tf_nd_solve_inv')
 
             def factor():
                 _lib.check(fac_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
                                   info.data_ptr(), _stream()), 'tf_nd_factor')
                 _lib.check(inv_fn(sp, fronts.data_ptr(), self.work.data_ptr(), wbytes, _stream()),
                            'tf_nd_invert')
-
-            def solve():
-                _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(),
-                                  self.scratch.data_ptr(), _stream()), 'tf_nd_solve_inv')
         else:
+            self.flow = None
             sol_fn = lib.tf_nd_solve_f64 if f64 else lib.tf_nd_solve_f32
 
             def factor():
@@ -248,11 +270,19 @@ class _Engine:
                            'tf_nd_solve')
 
         self.solve_raw = solve
+        self.lib = lib
         if graphs:
             self.factor = _Graphed(factor, solver.stats)
             self.solve = _Graphed(solve, solver.stats)
         else:
             self.factor, self.solve = factor, solve
+
+
+    def check(self):
+        """Raises when a bounded wait of the dataflow application gave up
+        since the last check (synchronising)."""
+        if self.flow is not None:
+            _lib.check(self.lib.tf_nd_flow_status(self.flow.data_ptr()), 'tf_nd_solve_flow')
 
 
 def _struct_ptr(s):
@@ -264,9 +294,14 @@ class Solver:
     """Per-interface solver state: the plan, factor buffers, Krylov workspace."""
 
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
-                 reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True):
+                 reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True, flow=False,
+                 flow_fuse_tiles=48, flow_chunk_tiles=24):
         self.itf = interface
         self.inverse = inverse
+        # dataflow application (one launch for both sweeps) of the inverted factors
+        self.flow = flow and inverse
+        self.flow_fuse_tiles = flow_fuse_tiles
+        self.flow_chunk_tiles = flow_chunk_tiles
         self.graphs = graphs
         self._engines = {}
         self.reuse = reuse
@@ -528,6 +563,8 @@ class Solver:
             self._axpby(1.0, b, -1.0, tmp, r)
         self.stats['gmres_iterations'] += its
         self.stats['last_relres'] = relres
+        if its and isinstance(fac, Factorization):
+            self._engine(fac.precision).check()
         if its:
             self._cost_iter = self._ema(self._cost_iter, (time.perf_counter() - t_start) / its)
         return x, its, relres
