@@ -64,6 +64,8 @@ def parse():
     ap.add_argument('--re', type=float, default=1000.0, help='Reynolds number of the --profile state')
     ap.add_argument('--apply', default='levels', choices=['flow', 'levels'],
                     help='application of the inverted factors: one dataflow launch or one launch per tree height')
+    ap.add_argument('--flow-fuse', type=int, default=48, help='dataflow apply: most factor tiles of a warp-task front')
+    ap.add_argument('--flow-chunk', type=int, default=24, help='dataflow apply: target tiles per CTA task')
     return ap.parse_args()
 
 
@@ -154,7 +156,8 @@ def gpu_arm(args, rank, world, local):
     torch.cuda.set_device(local)
     lib = _lib.load()
     params = {'CUDA': {'Factor Precision': args.precision, 'Tolerance': args.tol,
-                       'Dataflow Apply': args.apply == 'flow'}}
+                       'Dataflow Apply': args.apply == 'flow', 'Dataflow Fuse Tiles': args.flow_fuse,
+                       'Dataflow Chunk Tiles': args.flow_chunk}}
     itf = Interface(params, args.nx, args.nx, args.nz)
     n = itf.n
     stream = torch.cuda.current_stream()
@@ -435,7 +438,9 @@ def profile_stage(args):
     import torch
     from transiflow_gb300 import Interface
     p = {'Reynolds Number': args.re, 'CUDA': {'Factor Precision': args.precision, 'CUDA Graphs': False,
-                                              'Dataflow Apply': args.apply == 'flow'}}
+                                              'Dataflow Apply': args.apply == 'flow',
+                                              'Dataflow Fuse Tiles': args.flow_fuse,
+                                              'Dataflow Chunk Tiles': args.flow_chunk}}
     itf = Interface(p, args.nx, args.nx, args.nz)
     s = 0.1 * np.random.default_rng(1).standard_normal(itf.n)
     x = itf.vector_from_array(s)

@@ -122,7 +122,13 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(DevPlan P, int node0, int
         Bs[q][c] = (q < nb && c0 + c < f) ? F[(size_t)(k + q) * f + c0 + c] : T(0);
     }
     __syncthreads();
-    const int tr = (threadIdx.x / 16) * 4, tc = (threadIdx.x % 16) * 4;
+    // warp w owns rows [16 (w / 2), +16) and columns [32 (w % 2), +32) of the
+    // tile; a warp entirely past the front's edge skips its products (the FP64
+    // pipe is the bound, and the last tiles of a front are often partial)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wr = (warp >> 1) * 16, wc = (warp & 1) * 32;
+    if (r0 + wr >= f || c0 + wc >= f) return;
+    const int tr = wr + (lane >> 3) * 4, tc = wc + (lane & 7) * 4;
     T acc[4][4] = {};
 #pragma unroll 8
     for (int q = 0; q < NB; ++q) {

@@ -40,23 +40,32 @@ constexpr int FTHREADS = 32 * FW;
 constexpr int FSPT = 4;                // most 32-row strips per task
 constexpr int FLOW_SPIN = 1 << 22;     // polls before a wait gives up
 
-enum : int { K_FOWN = 0, K_FBND = 1, K_FALL = 2, K_BBND = 3, K_BOWN = 4, K_BALL = 5 };
+// Task kinds.  Split fronts: one CTA per task, a range of 32-row strips of
+// one part of a sweep.  Small fronts: bundles of up to FW fronts of one
+// height, one warp per front doing its whole sweep (r0 = number of fronts).
+enum : int { K_FOWN = 0, K_FBND = 1, K_BBND = 3, K_BOWN = 4, K_WFWD = 5, K_WBWD = 6 };
+constexpr int FUSE_F = 512;            // widest front a warp task takes
 
 struct FlowTask {
     int32_t node, kind, r0, r1;        // front rows [r0, r1) (split tasks)
     int32_t wait, target, signal, pad; // counter waited for (>= target) / incremented, -1: none
 };
 
+// Per-front counters of the bundles (the warp tasks read them per front).
+struct NodeFlow {
+    int32_t fw_wait, fw_target, fw_signal, bw_wait, bw_target, bw_signal, pad0, pad1;
+};
+
 // Device workspace: header, four counters per front, y/t values (one per
-// front index entry), tasks.  Bytes [FLOW_RESET_OFF, counters end) are cleared
-// before every application.
+// front index entry), per-front bundle counters, tasks.  Bytes
+// [FLOW_RESET_OFF, counters end) are cleared before every application.
 struct FlowHeader {
     int32_t err, ntasks, pad0, pad1;
-    int64_t tasks_off, ybuf_off;
+    int64_t tasks_off, ybuf_off, nodes_off;
     int32_t abort, ticket, pad2, pad3;
 };
-static_assert(sizeof(FlowHeader) == 48, "flow header layout");
-constexpr size_t FLOW_RESET_OFF = 32;
+static_assert(sizeof(FlowHeader) == 56, "flow header layout");
+constexpr size_t FLOW_RESET_OFF = 40;
 enum { C_FA = 0, C_KIDS = 1, C_BA = 2, C_BWD = 3 };   // counters of front i: 4 i + C_*
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
@@ -148,7 +157,7 @@ __device__ void products_prefetch(int kind, int n, int f, int R0, int ns, const 
 // vector holds column c at vec[c - vbase] (zero past its end, up to the
 // next multiple of 32).  `issued`: the first tile is already in flight.
 template <typename T>
-__device__ void products(int kind, int n, int f, int R0, int ns, const T *F, const T *vec, int vbase, T *tiles,
+__device__ __forceinline__ void products(int kind, int n, int f, int R0, int ns, const T *F, const T *vec, int vbase, T *tiles,
                          T *red, bool issued) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     T *buf0 = tiles + (2 * warp) * TILE, *buf1 = buf0 + TILE;
@@ -197,12 +206,44 @@ struct Front {
     double *y;
 };
 
-// Rows [Rb, Re) of one kind in chunks of FSPT strips: products, the sum over
-// warps, and the kind's update of x / y.  `out` (fused tasks) receives the
-// row results for the next part of the sweep.
 template <typename T>
-__device__ void run_rows(int kind, const Front<T> &fr, int Rb, int Re, const T *vec, int vbase, T *tiles, T *red,
-                         T *out, double *x, bool issued) {
+__device__ __forceinline__ Front<T> front_of(const DevPlan &P, int node, const T *fronts, const int32_t *piv,
+                                             double *ybuf) {
+    Front<T> fr;
+    fr.node = node;
+    fr.n = P.n_own[node];
+    fr.f = P.f[node];
+    fr.F = fronts + P.front_off[node];
+    fr.g = P.idx + P.idx_off[node];
+    fr.pv = piv + P.piv_off[node];
+    fr.y = ybuf + P.idx_off[node];
+    return fr;
+}
+
+// The kind's update of x / y for row r, given the row's product sum; `out`
+// (tasks doing both parts of a sweep) receives y or t for the next part.
+template <typename T>
+__device__ __forceinline__ void row_out(int kind, const Front<T> &fr, int r, T sum, T *out, double *x) {
+    if (kind == K_FOWN) {
+        const double yr = (double)sum + __ldcg(x + fr.g[fr.pv[r]]);
+        fr.y[r] = yr;
+        if (out) out[r] = (T)yr;
+    } else if (kind == K_FBND) {
+        atomicAdd(x + fr.g[r], -(double)sum);
+    } else if (kind == K_BBND) {
+        const double tr = __ldcg(fr.y + r) - (double)sum;
+        if (out) out[r] = (T)tr;
+        else fr.y[r] = tr;
+    } else {
+        x[fr.g[r]] = (double)sum;
+    }
+}
+
+// CTA task: rows [Rb, Re) of one kind in chunks of FSPT strips; products
+// shared by the warps, then the sum over warps.
+template <typename T>
+__device__ __forceinline__ void run_rows(int kind, const Front<T> &fr, int Rb, int Re, const T *vec, int vbase, T *tiles, T *red,
+                         double *x, bool issued) {
     for (int R0 = Rb; R0 < Re; R0 += FSPT * SB) {
         const int ns = min(FSPT, (Re - R0 + SB - 1) / SB);
         products(kind, fr.n, fr.f, R0, ns, fr.F, vec, vbase, tiles, red, issued && R0 == Rb);
@@ -215,39 +256,117 @@ __device__ void run_rows(int kind, const Front<T> &fr, int Rb, int Re, const T *
             for (int w = 0; w < FW; ++w) sum += red[(w * FSPT + s) * SB + l];
             const int r = R0 + s * SB + l;
             const int rhi = kind == K_FBND ? fr.f : fr.n;
-            if (r < min(Re, rhi)) {
-                if (kind == K_FOWN) {
-                    const double yr = (double)sum + __ldcg(x + fr.g[fr.pv[r]]);
-                    fr.y[r] = yr;
-                    if (out) out[r] = (T)yr;
-                } else if (kind == K_FBND) {
-                    atomicAdd(x + fr.g[r], -(double)sum);
-                } else if (kind == K_BBND) {
-                    const double tr = __ldcg(fr.y + r) - (double)sum;
-                    if (out) out[r] = (T)tr;
-                    else fr.y[r] = tr;
-                } else {
-                    x[fr.g[r]] = (double)sum;
-                }
-            }
+            if (r < min(Re, rhi)) row_out(kind, fr, r, sum, (T *)nullptr, x);
         }
         __syncthreads();
     }
 }
 
+// Warp task: all strips of rows [Rb, Re) of one kind by one warp, its tiles
+// double-buffered; lane l accumulates row Rb + 32 s + l of strip s.
+// `issued`: the first tile is already in flight.
 template <typename T>
-__global__ void __launch_bounds__(FTHREADS) flow_kernel(DevPlan P, const T *fronts, const int32_t *piv, double *x,
-                                                        char *work, int vlen) {
+__device__ __forceinline__ void warp_rows(int kind, const Front<T> &fr, int Rb, int Re, const T *vec, int vbase, T *buf0, T *buf1,
+                          T *out, double *x, bool issued) {
+    const int lane = threadIdx.x & 31;
+    const int nstr = (Re - Rb + SB - 1) / SB;
+    const int rhi = min(Re, kind == K_FBND ? fr.f : fr.n);
+    Cursor cur{kind, fr.n, fr.f, Rb, nstr, 0, 0};
+    int si = 0, ti = 0;
+    bool have = cur.locate(0, si, ti);
+    if (have && !issued) issue_item(kind, fr.n, fr.f, Rb, si, ti, fr.F, buf0, lane);
+    T acc = T(0);
+    int cs = 0;
+    for (int it = 0; have; ++it) {
+        for (; cs < si; ++cs) {
+            const int r = Rb + cs * SB + lane;
+            if (r < rhi) row_out(kind, fr, r, acc, out, x);
+            acc = T(0);
+        }
+        int sn = 0, tn = 0;
+        const bool more = cur.locate(it + 1, sn, tn);
+        if (more) {
+            issue_item(kind, fr.n, fr.f, Rb, sn, tn, fr.F, (it & 1) ? buf0 : buf1, lane);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncwarp();
+        const T *b = (it & 1) ? buf1 : buf0;
+        const Strip g = strip_of(kind, fr.n, fr.f, Rb + si * SB);
+        const T *v = vec + (g.c0 + ti * SB - vbase);
+        acc += ti == g.diag ? tile_dot_tri(b, v, lane, kind == K_FOWN) : tile_dot(b, v, lane);
+        __syncwarp();
+        have = more;
+        si = sn;
+        ti = tn;
+    }
+    for (; cs < nstr; ++cs) {
+        const int r = Rb + cs * SB + lane;
+        if (r < rhi) row_out(kind, fr, r, acc, out, x);
+        acc = T(0);
+    }
+}
+
+// Bounded wait of one thread; on giving up it raises the abort and error words.
+__device__ __forceinline__ void task_wait(FlowHeader *H, const int *ctr, int wait, int target) {
+    if (wait >= 0 && !flow_wait(ctr + wait, target, &H->abort)) {
+        atomicExch(&H->abort, 1);
+        atomicExch(&H->err, TF_ERR_TIMEOUT);
+    }
+    __threadfence();
+}
+
+// One small front's whole sweep by one warp (bundle tasks).
+template <typename T>
+__device__ __forceinline__ void warp_front(bool fwd, const Front<T> &fr, const NodeFlow &nf, FlowHeader *H, int *ctr, T *buf0,
+                           T *buf1, T *va, T *vb, double *x) {
+    const int lane = threadIdx.x & 31;
+    const int n = fr.n, f = fr.f;
+    const int k1 = fwd ? K_FOWN : K_BBND;
+    // the first tile does not depend on the wait
+    {
+        Cursor cur{k1, n, f, 0, (n + SB - 1) / SB, 0, 0};
+        int si, ti;
+        if (cur.locate(0, si, ti)) issue_item(k1, n, f, 0, si, ti, fr.F, buf0, lane);
+    }
+    if (lane == 0) task_wait(H, ctr, fwd ? nf.fw_wait : nf.bw_wait, fwd ? nf.fw_target : nf.bw_target);
+    __syncwarp();
+    const int padn = (n + SB - 1) / SB * SB;
+    for (int c = n + lane; c < padn; c += 32) vb[c] = T(0);
+    if (fwd) {
+        for (int c = lane; c < padn; c += 32) va[c] = c < n ? (T)__ldcg(x + fr.g[fr.pv[c]]) : T(0);
+        __syncwarp();
+        warp_rows(K_FOWN, fr, 0, n, va, 0, buf0, buf1, vb, x, true);
+        __syncwarp();
+        warp_rows(K_FBND, fr, n, f, vb, 0, buf0, buf1, (T *)nullptr, x, false);
+    } else {
+        const int len = f - n, pad = (len + SB - 1) / SB * SB;
+        for (int c = lane; c < pad; c += 32) va[c] = c < len ? (T)__ldcg(x + fr.g[n + c]) : T(0);
+        __syncwarp();
+        warp_rows(K_BBND, fr, 0, n, va, n, buf0, buf1, vb, x, true);
+        __syncwarp();
+        warp_rows(K_BOWN, fr, 0, n, vb, 0, buf0, buf1, (T *)nullptr, x, false);
+    }
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) atomicAdd(ctr + (fwd ? nf.fw_signal : nf.bw_signal), 1);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FTHREADS, 1) flow_kernel(DevPlan P, const T *fronts, const int32_t *piv, double *x,
+                                                        char *work) {
     extern __shared__ unsigned char smem_raw[];
     T *tiles = reinterpret_cast<T *>(smem_raw);   // [FW][2] tiles
     T *red = tiles + 2 * FW * TILE;                // [FW][FSPT][32]
-    T *va = red + FW * FSPT * SB;                  // [vlen]
-    T *vb = va + vlen;                             // [vlen]
+    T *vec = red + FW * FSPT * SB;                 // CTA tasks: [vlen]; bundles: [FW][2][FUSE_F]
     FlowHeader *H = reinterpret_cast<FlowHeader *>(work);
     int *ctr = reinterpret_cast<int *>(work + sizeof(FlowHeader));
     const int ntasks = H->ntasks;
     const FlowTask *tasks = reinterpret_cast<const FlowTask *>(work + H->tasks_off);
+    const NodeFlow *nodes = reinterpret_cast<const NodeFlow *>(work + H->nodes_off);
     double *ybuf = reinterpret_cast<double *>(work + H->ybuf_off);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ int s_ticket;
     for (;;) {
         if (threadIdx.x == 0) s_ticket = atomicAdd(&H->ticket, 1);
@@ -255,60 +374,47 @@ __global__ void __launch_bounds__(FTHREADS) flow_kernel(DevPlan P, const T *fron
         const int ti = s_ticket;
         if (ti >= ntasks) break;
         const FlowTask tk = tasks[ti];
-        Front<T> fr;
-        fr.node = tk.node;
-        fr.n = P.n_own[fr.node];
-        fr.f = P.f[fr.node];
-        fr.F = fronts + P.front_off[fr.node];
-        fr.g = P.idx + P.idx_off[fr.node];
-        fr.pv = piv + P.piv_off[fr.node];
-        fr.y = ybuf + P.idx_off[fr.node];
-        const int n = fr.n, f = fr.f;
-        const bool fused = tk.kind == K_FALL || tk.kind == K_BALL;
-        const int k1 = tk.kind == K_FALL ? K_FOWN : tk.kind == K_BALL ? K_BBND : tk.kind;
-        const int Rb = fused ? 0 : tk.r0;
-        const int Re = fused ? n : tk.r1;
-        products_prefetch(k1, n, f, Rb, min(FSPT, (Re - Rb + SB - 1) / SB), fr.F, tiles);
-        if (threadIdx.x == 0 && tk.wait >= 0) {
-            if (!flow_wait(ctr + tk.wait, tk.target, &H->abort)) {
-                atomicExch(&H->abort, 1);
-                atomicExch(&H->err, TF_ERR_TIMEOUT);
+        if (tk.kind == K_WFWD || tk.kind == K_WBWD) {
+            // a bundle of up to FW small fronts of one height, one per warp
+            if (warp < tk.r0) {
+                const int node = tk.node + warp;
+                const Front<T> fr = front_of(P, node, fronts, piv, ybuf);
+                T *b0 = tiles + (2 * warp) * TILE;
+                T *va = vec + (2 * warp) * FUSE_F;
+                warp_front(tk.kind == K_WFWD, fr, nodes[node], H, ctr, b0, b0 + TILE, va, va + FUSE_F, x);
             }
-            __threadfence();
+            __syncthreads();
+            continue;
         }
+        const Front<T> fr = front_of(P, tk.node, fronts, piv, ybuf);
+        const int n = fr.n, f = fr.f;
+        const int kind = tk.kind, Rb = tk.r0, Re = tk.r1;
+        products_prefetch(kind, n, f, Rb, min(FSPT, (Re - Rb + SB - 1) / SB), fr.F, tiles);
+        if (threadIdx.x == 0) task_wait(H, ctr, tk.wait, tk.target);
         __syncthreads();
-        // the vector of the first part (zero past its end, to the next tile)
+        // the task's vector, zero past its end up to the next tile
         int vbase = 0;
-        if (k1 == K_FOWN) {
-            const int len = Re, pad = (len + SB - 1) / SB * SB;
+        if (kind == K_FOWN) {
+            const int pad = (Re + SB - 1) / SB * SB;
             for (int c = threadIdx.x; c < pad; c += FTHREADS)
-                va[c] = c < len ? (T)__ldcg(x + fr.g[fr.pv[c]]) : T(0);
-        } else if (k1 == K_FBND) {
+                vec[c] = c < Re ? (T)__ldcg(x + fr.g[fr.pv[c]]) : T(0);
+        } else if (kind == K_FBND) {
             const int pad = (n + SB - 1) / SB * SB;
-            for (int c = threadIdx.x; c < pad; c += FTHREADS) va[c] = c < n ? (T)__ldcg(fr.y + c) : T(0);
-        } else if (k1 == K_BBND) {
+            for (int c = threadIdx.x; c < pad; c += FTHREADS) vec[c] = c < n ? (T)__ldcg(fr.y + c) : T(0);
+        } else if (kind == K_BBND) {
             const int len = f - n, pad = (len + SB - 1) / SB * SB;
             vbase = n;
-            for (int c = threadIdx.x; c < pad; c += FTHREADS) va[c] = c < len ? (T)__ldcg(x + fr.g[n + c]) : T(0);
+            for (int c = threadIdx.x; c < pad; c += FTHREADS) vec[c] = c < len ? (T)__ldcg(x + fr.g[n + c]) : T(0);
         } else {
             const int pad = (n + SB - 1) / SB * SB;
-            for (int c = Rb + threadIdx.x; c < pad; c += FTHREADS) va[c] = c < n ? (T)__ldcg(fr.y + c) : T(0);
+            for (int c = Rb + threadIdx.x; c < pad; c += FTHREADS) vec[c] = c < n ? (T)__ldcg(fr.y + c) : T(0);
         }
         __syncthreads();
-        if (!fused) {
-            run_rows(k1, fr, Rb, Re, va, vbase, tiles, red, (T *)nullptr, x, true);
-        } else {
-            // first part: y (forward) or t (backward) of all own rows into vb
-            for (int c = n + threadIdx.x; c < (n + SB - 1) / SB * SB; c += FTHREADS) vb[c] = T(0);
-            run_rows(k1, fr, 0, n, va, vbase, tiles, red, vb, x, true);
-            if (tk.kind == K_FALL)
-                run_rows(K_FBND, fr, n, f, vb, 0, tiles, red, (T *)nullptr, x, false);
-            else
-                run_rows(K_BOWN, fr, 0, n, vb, 0, tiles, red, (T *)nullptr, x, false);
-        }
+        run_rows(kind, fr, Rb, Re, vec, vbase, tiles, red, x, true);
         __threadfence();
         __syncthreads();
         if (threadIdx.x == 0 && tk.signal >= 0) atomicAdd(ctr + tk.signal, 1);
+        (void)lane;
     }
 }
 
@@ -362,17 +468,18 @@ static void chunks(int kind, int n, int f, int chunk, std::vector<std::pair<int,
 }
 
 static int flow_build(const tf_nd_plan *p, const FlowPlanHost &h, int fuse_tiles, int chunk_tiles,
-                      std::vector<FlowTask> &tasks) {
+                      std::vector<FlowTask> &tasks, std::vector<NodeFlow> &nodes) {
     const int nn = p->nnodes;
     if (chunk_tiles < 1) chunk_tiles = 1;
     std::vector<int> ep(nn, -1);
     for (int i = 0; i < nn; ++i) {
+        if (h.n[i] < 0 || h.f[i] < h.n[i]) return TF_ERR_ARG;
         int a = h.parent[i];
         while (a >= 0 && h.n[a] == 0) a = h.parent[a];
         ep[i] = a;
         if (h.n[i] > 0 && h.f[i] > h.n[i] && a < 0) return TF_ERR_ARG;   // boundary rows need an ancestor
-        if (h.n[i] < 0 || h.f[i] < h.n[i]) return TF_ERR_ARG;
     }
+    // small fronts go to warp tasks; the others are split into CTA tasks
     std::vector<char> fused(nn, 0);
     std::vector<std::vector<std::pair<int, int>>> ch(4 * (size_t)nn);   // per front: FOWN, FBND, BBND, BOWN
     const int kinds[4] = {K_FOWN, K_FBND, K_BBND, K_BOWN};
@@ -381,11 +488,11 @@ static int flow_build(const tf_nd_plan *p, const FlowPlanHost &h, int fuse_tiles
         if (n == 0) continue;
         const int64_t no = (n + SB - 1) / SB, nb = (f - n + SB - 1) / SB;
         const int64_t sweep = no * (no + 1) / 2 + no * nb;
-        fused[i] = fuse_tiles > 0 && sweep <= fuse_tiles;
+        fused[i] = fuse_tiles > 0 && sweep <= fuse_tiles && f <= FUSE_F;
         if (fused[i]) continue;
         for (int k = 0; k < 4; ++k) chunks(kinds[k], n, f, chunk_tiles, ch[4 * (size_t)i + k]);
     }
-    // finishing tasks of each sweep and the forward targets of the parents
+    // tasks finishing each sweep of a front; forward targets of the parents
     auto nfwd_fin = [&](int i) -> int {
         if (fused[i]) return 1;
         return (int)(h.f[i] > h.n[i] ? ch[4 * (size_t)i + 1].size() : ch[4 * (size_t)i].size());
@@ -394,6 +501,19 @@ static int flow_build(const tf_nd_plan *p, const FlowPlanHost &h, int fuse_tiles
     std::vector<int> kids(nn, 0);
     for (int i = 0; i < nn; ++i)
         if (h.n[i] > 0 && h.f[i] > h.n[i]) kids[ep[i]] += nfwd_fin(i);
+    // the counters of a front: forward waits for its children, backward for
+    // its parent (without boundary: for its own forward)
+    nodes.assign(nn, NodeFlow{});
+    for (int i = 0; i < nn; ++i) {
+        NodeFlow &nf = nodes[i];
+        const bool bnd = h.f[i] > h.n[i];
+        nf.fw_target = kids[i];
+        nf.fw_wait = kids[i] > 0 ? 4 * i + C_KIDS : -1;
+        nf.fw_signal = bnd ? 4 * ep[i] + C_KIDS : 4 * i + C_FA;
+        nf.bw_wait = bnd ? 4 * ep[i] + C_BWD : 4 * i + C_FA;
+        nf.bw_target = h.n[i] == 0 ? 0 : bnd ? nbwd_fin(ep[i]) : nfwd_fin(i);
+        nf.bw_signal = 4 * i + C_BWD;
+    }
     tasks.clear();
     auto push = [&](int node, int kind, int r0, int r1, int wait, int target, int signal) {
         FlowTask t;
@@ -401,17 +521,25 @@ static int flow_build(const tf_nd_plan *p, const FlowPlanHost &h, int fuse_tiles
         t.wait = target > 0 ? wait : -1; t.target = target; t.signal = signal; t.pad = 0;
         tasks.push_back(t);
     };
-    // forward, leaves first; per height the own-row tasks of all fronts, then
-    // their boundary tasks
+    // consecutive small fronts of one height, at most FW per bundle
+    auto bundles = [&](int a, int b, int kind) {
+        for (int i = a; i < b;) {
+            if (h.n[i] == 0 || !fused[i]) { ++i; continue; }
+            int j = i;
+            while (j < b && j - i < FW && h.n[j] > 0 && fused[j]) ++j;
+            push(i, kind, j - i, 0, -1, 0, -1);
+            i = j;
+        }
+    };
+    // forward, leaves first; per height the bundles, the own-row tasks of the
+    // split fronts, then their boundary tasks
     for (int lv = 0; lv < p->nlevels; ++lv) {
         const int a = p->level_ptr[lv], b = p->level_ptr[lv + 1];
+        bundles(a, b, K_WFWD);
         for (int i = a; i < b; ++i) {
-            if (h.n[i] == 0) continue;
-            const bool bnd = h.f[i] > h.n[i];
-            const int fin_sig = bnd ? 4 * ep[i] + C_KIDS : 4 * i + C_FA;
-            if (fused[i]) push(i, K_FALL, 0, h.n[i], 4 * i + C_KIDS, kids[i], fin_sig);
-            else
-                for (auto &c : ch[4 * (size_t)i]) push(i, K_FOWN, c.first, c.second, 4 * i + C_KIDS, kids[i], 4 * i + C_FA);
+            if (h.n[i] == 0 || fused[i]) continue;
+            for (auto &c : ch[4 * (size_t)i])
+                push(i, K_FOWN, c.first, c.second, nodes[i].fw_wait, nodes[i].fw_target, 4 * i + C_FA);
         }
         for (int i = a; i < b; ++i) {
             if (h.n[i] == 0 || fused[i]) continue;
@@ -420,24 +548,20 @@ static int flow_build(const tf_nd_plan *p, const FlowPlanHost &h, int fuse_tiles
                 push(i, K_FBND, c.first, c.second, 4 * i + C_FA, nfa, 4 * ep[i] + C_KIDS);
         }
     }
-    // backward, root first; a front waits for its parent's backward (or, with
-    // no boundary, for its own forward)
+    // backward, root first
     for (int lv = p->nlevels - 1; lv >= 0; --lv) {
         const int a = p->level_ptr[lv], b = p->level_ptr[lv + 1];
         for (int i = a; i < b; ++i) {
-            if (h.n[i] == 0) continue;
-            const bool bnd = h.f[i] > h.n[i];
-            const int w = bnd ? 4 * ep[i] + C_BWD : 4 * i + C_FA;
-            const int tgt = bnd ? nbwd_fin(ep[i]) : nfwd_fin(i);
-            if (fused[i]) push(i, K_BALL, 0, h.n[i], w, tgt, 4 * i + C_BWD);
-            else
-                for (auto &c : ch[4 * (size_t)i + 2]) push(i, K_BBND, c.first, c.second, w, tgt, 4 * i + C_BA);
+            if (h.n[i] == 0 || fused[i]) continue;
+            for (auto &c : ch[4 * (size_t)i + 2])
+                push(i, K_BBND, c.first, c.second, nodes[i].bw_wait, nodes[i].bw_target, 4 * i + C_BA);
         }
         for (int i = a; i < b; ++i) {
             if (h.n[i] == 0 || fused[i]) continue;
             const int nba = (int)ch[4 * (size_t)i + 2].size();
             for (auto &c : ch[4 * (size_t)i + 3]) push(i, K_BOWN, c.first, c.second, 4 * i + C_BA, nba, 4 * i + C_BWD);
         }
+        bundles(a, b, K_WBWD);
     }
     return TF_OK;
 }
@@ -445,27 +569,28 @@ static int flow_build(const tf_nd_plan *p, const FlowPlanHost &h, int fuse_tiles
 static size_t align16(size_t b) { return (b + 15) / 16 * 16; }
 
 struct FlowLayout {
-    size_t ctr_off, ybuf_off, tasks_off, total;
+    size_t ctr_off, ybuf_off, nodes_off, tasks_off, total;
 };
 
 static FlowLayout flow_layout(int nnodes, int64_t idx_total, size_t ntasks) {
     FlowLayout L;
     L.ctr_off = sizeof(FlowHeader);
     L.ybuf_off = align16(L.ctr_off + 16 * (size_t)nnodes);
-    L.tasks_off = align16(L.ybuf_off + 8 * (size_t)idx_total);
+    L.nodes_off = align16(L.ybuf_off + 8 * (size_t)idx_total);
+    L.tasks_off = align16(L.nodes_off + sizeof(NodeFlow) * (size_t)nnodes);
     L.total = L.tasks_off + sizeof(FlowTask) * ntasks;
     return L;
 }
 
-static int vlen_of(const tf_nd_plan *p) {
+// Shared memory: the warps' tile buffers, the CTA tasks' partial sums, and a
+// vector area holding a CTA task's vector (the widest front) or the bundles'
+// two vectors per warp.
+template <typename T>
+static size_t flow_smem(const tf_nd_plan *p) {
     int m = 0;
     for (int h = 0; h < p->nlevels; ++h) m = std::max(m, p->max_f[h]);
-    return (m + SB - 1) / SB * SB;
-}
-
-template <typename T>
-static size_t flow_smem(int vlen) {
-    return sizeof(T) * ((size_t)2 * FW * TILE + (size_t)FW * FSPT * SB + 2 * (size_t)vlen);
+    const size_t vlen = std::max((size_t)(m + SB - 1) / SB * SB, (size_t)2 * FW * FUSE_F);
+    return sizeof(T) * ((size_t)2 * FW * TILE + (size_t)FW * FSPT * SB + vlen);
 }
 
 template <typename T>
@@ -474,8 +599,7 @@ static int solve_flow(const tf_nd_plan *p, const T *fronts, const int32_t *piv, 
     int e = check_plan(p);
     if (e) return e;
     if (!fronts || !piv || !x || !work) return TF_ERR_ARG;
-    const int vlen = vlen_of(p);
-    const size_t smem = flow_smem<T>(vlen);
+    const size_t smem = flow_smem<T>(p);
     if ((e = ensure_smem((const void *)flow_kernel<T>, smem))) return e;
     int dev = 0, nsm = 0, occ = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -488,7 +612,7 @@ static int solve_flow(const tf_nd_plan *p, const T *fronts, const int32_t *piv, 
         cudaSuccess)
         return TF_ERR_CUDA;
     const DevPlan D = dev_plan(p, p->d_rank);
-    flow_kernel<T><<<nsm * occ, FTHREADS, smem, s>>>(D, fronts, piv, x, w, vlen);
+    flow_kernel<T><<<nsm * occ, FTHREADS, smem, s>>>(D, fronts, piv, x, w);
     launched();
     return cuda_status();
 }
@@ -503,7 +627,8 @@ extern "C" size_t tf_nd_flow_workspace_bytes(const tf_nd_plan *plan, int fuse_ti
     nd::FlowPlanHost h;
     if (nd::flow_read_plan(plan, h)) return 0;
     std::vector<nd::FlowTask> tasks;
-    if (nd::flow_build(plan, h, fuse_tiles, chunk_tiles, tasks)) return 0;
+    std::vector<nd::NodeFlow> nodes;
+    if (nd::flow_build(plan, h, fuse_tiles, chunk_tiles, tasks, nodes)) return 0;
     return nd::flow_layout(plan->nnodes, h.idx_total, tasks.size()).total;
 }
 
@@ -513,23 +638,26 @@ extern "C" int tf_nd_flow_prepare(const tf_nd_plan *plan, void *d_work, size_t w
     if (e) return e;
     if (!d_work || (elem_size != 4 && elem_size != 8)) return TF_ERR_ARG;
     // the launch needs its shared memory: refuse here rather than at the first solve
-    const int vlen = nd::vlen_of(plan);
-    e = elem_size == 8 ? nd::ensure_smem((const void *)nd::flow_kernel<double>, nd::flow_smem<double>(vlen))
-                       : nd::ensure_smem((const void *)nd::flow_kernel<float>, nd::flow_smem<float>(vlen));
+    e = elem_size == 8 ? nd::ensure_smem((const void *)nd::flow_kernel<double>, nd::flow_smem<double>(plan))
+                       : nd::ensure_smem((const void *)nd::flow_kernel<float>, nd::flow_smem<float>(plan));
     if (e) return e;
     nd::FlowPlanHost h;
     if ((e = nd::flow_read_plan(plan, h))) return e;
     std::vector<nd::FlowTask> tasks;
-    if ((e = nd::flow_build(plan, h, fuse_tiles, chunk_tiles, tasks))) return e;
+    std::vector<nd::NodeFlow> nodes;
+    if ((e = nd::flow_build(plan, h, fuse_tiles, chunk_tiles, tasks, nodes))) return e;
     const nd::FlowLayout L = nd::flow_layout(plan->nnodes, h.idx_total, tasks.size());
     if (work_bytes < L.total) return TF_ERR_SIZE;
     nd::FlowHeader hd = {};
     hd.ntasks = (int32_t)tasks.size();
     hd.tasks_off = (int64_t)L.tasks_off;
     hd.ybuf_off = (int64_t)L.ybuf_off;
+    hd.nodes_off = (int64_t)L.nodes_off;
     char *w = static_cast<char *>(d_work);
     if (cudaMemcpy(w, &hd, sizeof(hd), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(w + L.ctr_off, 0, L.ybuf_off - L.ctr_off) != cudaSuccess ||
+        cudaMemcpy(w + L.nodes_off, nodes.data(), sizeof(nd::NodeFlow) * nodes.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
         cudaMemcpy(w + L.tasks_off, tasks.data(), sizeof(nd::FlowTask) * tasks.size(), cudaMemcpyHostToDevice) !=
             cudaSuccess)
         return TF_ERR_CUDA;
