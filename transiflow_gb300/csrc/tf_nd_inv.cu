@@ -236,39 +236,41 @@ static int invert(const tf_nd_plan *p, const DevPlan &D, T *fronts, T *work, siz
 }
 
 // ---------------------------------------------------------------------------
-// Application with the inverted blocks.
+// Application with the inverted blocks.  Per height, two launches per sweep:
+//   forward   y = s + L11^-1 s into the scratch (s: the front's own rows of x
+//             in pivot order, gathered by each CTA), then x[bnd] -= L21 y;
+//   backward  t = y - U12 x[bnd] in the scratch, then x[own] = U11^-1 t.
+// x's own rows are written only by the backward product, so no launch reads
+// rows another CTA of the same launch writes.
 // ---------------------------------------------------------------------------
-constexpr int VT = 128;            // threads per CTA of the gather
-constexpr int VW = 8;              // rows (one warp each) per CTA of the products
+constexpr int VT = 128;            // rows (one thread each) per CTA of the row kernel
+constexpr int VW = 8;              // rows (one warp each) per CTA of the warp kernel
 
-// packed[idx_off + c] = x[g[pv[c]]] (forward, with the row permutation) or
-// x[g[c]] (backward) for the own rows of every front of one height: each
-// front's right-hand side contiguous for the products below.
-template <bool FWD>
-__global__ void __launch_bounds__(VT) inv_gather_kernel(DevPlan P, int node0, const int32_t *piv, const double *x,
-                                                        double *packed) {
-    const int node = node0 + blockIdx.y;
-    const int n = P.n_own[node];
-    const int c = blockIdx.x * VT + threadIdx.x;
-    if (c >= n) return;
-    const int32_t *g = P.idx + P.idx_off[node];
-    packed[P.idx_off[node] + c] = FWD ? x[g[piv[P.piv_off[node] + c]]] : x[g[c]];
-}
-
-// x[g[r]] = (L11^-1 s)_r (forward; unit diagonal) or (U11^-1 s)_r
-// (backward) for the own rows: one warp per row, lanes over the columns
-// (coalesced reads of the row and of s), then a shuffle sum.  The shuffle
-// costs five FP64 adds per row against the row's length / 32 products per
-// lane; in exchange the large fronts near the root spread over many SMs.
+// One warp per row, lanes over the columns (coalesced reads of the row and
+// of s), then a shuffle sum: five FP64 adds per row against the row's
+// length / 32 products per lane, in exchange for spreading the large fronts
+// near the root over many SMs.
 template <typename T, bool FWD>
 __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0, const T *fronts,
-                                                            const double *packed, double *x) {
+                                                            const int32_t *piv, double *x, double *packed) {
+    extern __shared__ double s_gather[];   // forward: s[0 .. rmax)
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
+    const int rfirst = blockIdx.x * VW;
+    if (rfirst >= n) return;
+    const int32_t *g = P.idx + P.idx_off[node];
+    double *pk = packed + P.idx_off[node];
+    const double *sv = pk;
+    if (FWD) {
+        const int rmax = min(n, rfirst + VW);
+        const int32_t *pv = piv + P.piv_off[node];
+        for (int c = threadIdx.x; c < rmax; c += 32 * VW) s_gather[c] = x[g[pv[c]]];
+        __syncthreads();
+        sv = s_gather;
+    }
     const int lane = threadIdx.x & 31;
-    const int r = blockIdx.x * VW + (threadIdx.x >> 5);
+    const int r = rfirst + (threadIdx.x >> 5);
     if (r >= n) return;
-    const double *sv = packed + P.idx_off[node];
     const T *row = fronts + P.front_off[node] + (size_t)r * f;
     const int c0 = FWD ? 0 : r, c1 = FWD ? r : n;
     T s0 = T(0), s1 = T(0);
@@ -282,25 +284,35 @@ __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (lane == 0) {
-        const int32_t *g = P.idx + P.idx_off[node];
-        x[g[r]] = FWD ? (double)s + sv[r] : (double)s;
+        if (FWD) pk[r] = (double)s + sv[r];
+        else x[g[r]] = (double)s;
     }
 }
 
-// The same product with one row per thread, for FP64 heights whose own
-// blocks are short (the leaves): a warp's rows would be too short to pay for
-// its FP64 shuffle sum.  Threads of a warp read the same s[c] (a broadcast) and their
-// own rows through the L1 cache.
+// The same product with one row per thread, for FP64 heights with many
+// fronts whose own blocks are short (the leaves): there a warp's rows would
+// be too short to pay for its FP64 shuffle sum, and the fronts alone fill the
+// GPU.  Threads of a warp read the same s[c] (a broadcast) and their own rows
+// through the L1 cache.
 constexpr int VS = 128;            // own rows up to which a thread takes a row
 
 template <typename T, bool FWD>
 __global__ void __launch_bounds__(VT) inv_apply_rows_kernel(DevPlan P, int node0, const T *fronts,
-                                                            const double *packed, double *x) {
+                                                            const int32_t *piv, double *x, double *packed) {
+    __shared__ double s_gather[VS];
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
-    const int r = blockIdx.x * VT + threadIdx.x;
+    const int32_t *g = P.idx + P.idx_off[node];
+    double *pk = packed + P.idx_off[node];
+    const double *sv = pk;
+    if (FWD) {
+        const int32_t *pv = piv + P.piv_off[node];
+        for (int c = threadIdx.x; c < n; c += VT) s_gather[c] = x[g[pv[c]]];
+        __syncthreads();
+        sv = s_gather;
+    }
+    const int r = threadIdx.x;
     if (r >= n) return;
-    const double *sv = packed + P.idx_off[node];
     const T *row = fronts + P.front_off[node] + (size_t)r * f;
     const int c0 = FWD ? 0 : r, c1 = FWD ? r : n;
     T s0 = T(0), s1 = T(0);
@@ -310,41 +322,119 @@ __global__ void __launch_bounds__(VT) inv_apply_rows_kernel(DevPlan P, int node0
         s1 += row[c + 1] * (T)sv[c + 1];
     }
     if (c < c1) s0 += row[c] * (T)sv[c];
+    if (FWD) pk[r] = (double)(s0 + s1) + sv[r];
+    else x[g[r]] = (double)(s0 + s1);
+}
+
+// Boundary couplings: forward x[bnd] -= L21 y (y from the scratch), backward
+// t[own] -= U12 x[bnd] (into the scratch).  One 32-row by (32 ctiles)-column
+// piece per warp (grid: row pieces x fronts x column pieces), tiles double
+// buffered in shared memory, every lane one row; pieces of one row add
+// through atomics.  Heights with few fronts take one tile per piece, so that
+// their few large fronts still spread over many SMs.
+constexpr int BV_WARPS = 2;
+constexpr int BV_THREADS = 32 * BV_WARPS;
+constexpr int BV_ROWS = 32 * BV_WARPS;
+constexpr int BV_TILES = 4;        // most column tiles per piece
+
+template <typename T, bool FWD>
+__global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node0, int ctiles, const T *fronts,
+                                                             double *x, double *packed) {
+    extern __shared__ unsigned char smem_raw[];
+    T *tiles = reinterpret_cast<T *>(smem_raw);   // [BV_WARPS][2] tiles
+    __shared__ T v[BV_TILES * SB];
+    const int node = node0 + blockIdx.y;
+    const int n = P.n_own[node], f = P.f[node];
+    const int rlo = FWD ? n : 0, rhi = FWD ? f : n;
+    const int clo = FWD ? 0 : n, chi = FWD ? n : f;
+    const int ccols = ctiles * SB;
+    const int rbase = rlo + blockIdx.x * BV_ROWS;
+    const int cbase = clo + blockIdx.z * ccols;
+    if (rbase >= rhi || cbase >= chi) return;
+    const int cend = min(chi, cbase + ccols);
+    const T *F = fronts + P.front_off[node];
     const int32_t *g = P.idx + P.idx_off[node];
-    x[g[r]] = FWD ? (double)(s0 + s1) + sv[r] : (double)(s0 + s1);
+    double *pk = packed + P.idx_off[node];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r0 = rbase + warp * SB;
+    T *b0 = tiles + (2 * warp) * TILE, *b1 = b0 + TILE;
+    if (r0 < rhi) tile_issue(b0, F, f, r0, rhi, cbase, chi, lane);
+    for (int c = threadIdx.x; c < ccols; c += BV_THREADS)
+        v[c] = cbase + c < cend ? (T)(FWD ? pk[cbase + c] : x[g[cbase + c]]) : T(0);
+    __syncthreads();
+    if (r0 >= rhi) return;
+    T s = T(0);
+    int t = 0;
+    for (int c0 = cbase; c0 < cend; c0 += SB, ++t) {
+        T *cur = (t & 1) ? b1 : b0;
+        if (c0 + SB < cend) {
+            tile_issue((t & 1) ? b0 : b1, F, f, r0, rhi, c0 + SB, chi, lane);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncwarp();
+        s += tile_dot(cur, v + (c0 - cbase), lane);
+        __syncwarp();
+    }
+    if (r0 + lane < rhi) {
+        if (FWD) atomicAdd(x + g[r0 + lane], -(double)s);
+        else atomicAdd(pk + r0 + lane, -(double)s);
+    }
 }
 
 template <typename T, bool FWD>
-static void inv_apply(const DevPlan &D, int node0, int cnt, int mo, const T *fronts, const double *packed, double *x,
-                      cudaStream_t s) {
+static int inv_apply(const DevPlan &D, int node0, int cnt, int mo, const T *fronts, const int32_t *piv, double *x,
+                     double *packed, cudaStream_t s) {
     // FP32 shuffles are cheap, so single precision always takes a warp per row
-    if (sizeof(T) == 8 && mo <= VS)
-        inv_apply_rows_kernel<T, FWD><<<dim3((mo + VT - 1) / VT, cnt), VT, 0, s>>>(D, node0, fronts, packed, x);
-    else
-        inv_apply_kernel<T, FWD><<<dim3((mo + VW - 1) / VW, cnt), 32 * VW, 0, s>>>(D, node0, fronts, packed, x);
+    if (sizeof(T) == 8 && mo <= VS && cnt >= 256) {
+        inv_apply_rows_kernel<T, FWD><<<dim3(1, cnt), VT, 0, s>>>(D, node0, fronts, piv, x, packed);
+    } else {
+        const size_t sm = FWD ? sizeof(double) * (size_t)mo : 0;
+        if (sm > 48 * 1024) {
+            const int e = ensure_smem((const void *)inv_apply_kernel<T, FWD>, sm);
+            if (e) return e;
+        }
+        inv_apply_kernel<T, FWD><<<dim3((mo + VW - 1) / VW, cnt), 32 * VW, sm, s>>>(D, node0, fronts, piv, x,
+                                                                                   packed);
+    }
+    launched();
+    return TF_OK;
+}
+
+template <typename T, bool FWD>
+static void inv_bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, int nsm, const T *fronts, double *x,
+                    double *packed, cudaStream_t s) {
+    if (rows <= 0 || cols <= 0) return;
+    const int rb = (rows + BV_ROWS - 1) / BV_ROWS;
+    const int wide = rb * cnt * ((cols + BV_TILES * SB - 1) / (BV_TILES * SB));
+    const int ctiles = wide >= 4 * nsm ? BV_TILES : 1;
+    dim3 grid(rb, cnt, (cols + ctiles * SB - 1) / (ctiles * SB));
+    inv_bnd_kernel<T, FWD><<<grid, BV_THREADS, sizeof(T) * 2 * BV_WARPS * TILE, s>>>(D, node0, ctiles, fronts, x,
+                                                                                     packed);
     launched();
 }
 
 template <typename T>
 static int solve_inv(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int32_t *piv, double *x,
                      double *packed, cudaStream_t s) {
+    int dev = 0, nsm = 0, e = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return TF_ERR_CUDA;
     for (int h = 0; h < p->nlevels; ++h) {
         const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
         const int mo = p->max_own[h], mf = p->max_f[h];
         if (cnt <= 0 || mo <= 0) continue;
-        inv_gather_kernel<true><<<dim3((mo + VT - 1) / VT, cnt), VT, 0, s>>>(D, node0, piv, x, packed);
-        launched();
-        inv_apply<T, true>(D, node0, cnt, mo, fronts, packed, x, s);
-        bnd<T, true>(D, node0, cnt, mf, mo, fronts, x, s);
+        if ((e = inv_apply<T, true>(D, node0, cnt, mo, fronts, piv, x, packed, s))) return e;
+        inv_bnd<T, true>(D, node0, cnt, mf, mo, nsm, fronts, x, packed, s);
     }
     for (int h = p->nlevels - 1; h >= 0; --h) {
         const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
         const int mo = p->max_own[h], mf = p->max_f[h];
         if (cnt <= 0 || mo <= 0) continue;
-        bnd<T, false>(D, node0, cnt, mo, mf, fronts, x, s);
-        inv_gather_kernel<false><<<dim3((mo + VT - 1) / VT, cnt), VT, 0, s>>>(D, node0, piv, x, packed);
-        launched();
-        inv_apply<T, false>(D, node0, cnt, mo, fronts, packed, x, s);
+        inv_bnd<T, false>(D, node0, cnt, mo, mf, nsm, fronts, x, packed, s);
+        if ((e = inv_apply<T, false>(D, node0, cnt, mo, fronts, piv, x, packed, s))) return e;
     }
     return cuda_status();
 }
