@@ -66,6 +66,7 @@ def parse():
                     help='application of the inverted factors: one dataflow launch or one launch per tree height')
     ap.add_argument('--flow-fuse', type=int, default=48, help='dataflow apply: most factor tiles of a warp-task front')
     ap.add_argument('--flow-chunk', type=int, default=24, help='dataflow apply: target tiles per CTA task')
+    ap.add_argument('--leaf-cells', type=int, default=48, help='grid cells at which nested dissection stops')
     return ap.parse_args()
 
 
@@ -157,7 +158,7 @@ def gpu_arm(args, rank, world, local):
     lib = _lib.load()
     params = {'CUDA': {'Factor Precision': args.precision, 'Tolerance': args.tol,
                        'Dataflow Apply': args.apply == 'flow', 'Dataflow Fuse Tiles': args.flow_fuse,
-                       'Dataflow Chunk Tiles': args.flow_chunk}}
+                       'Dataflow Chunk Tiles': args.flow_chunk, 'Leaf Cells': args.leaf_cells}}
     itf = Interface(params, args.nx, args.nx, args.nz)
     n = itf.n
     stream = torch.cuda.current_stream()
@@ -440,7 +441,7 @@ def profile_stage(args):
     p = {'Reynolds Number': args.re, 'CUDA': {'Factor Precision': args.precision, 'CUDA Graphs': False,
                                               'Dataflow Apply': args.apply == 'flow',
                                               'Dataflow Fuse Tiles': args.flow_fuse,
-                                              'Dataflow Chunk Tiles': args.flow_chunk}}
+                                              'Dataflow Chunk Tiles': args.flow_chunk, 'Leaf Cells': args.leaf_cells}}
     itf = Interface(p, args.nx, args.nx, args.nz)
     s = 0.1 * np.random.default_rng(1).standard_normal(itf.n)
     x = itf.vector_from_array(s)

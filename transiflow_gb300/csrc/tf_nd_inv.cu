@@ -84,12 +84,15 @@ __global__ void __launch_bounds__(32) inv_diag_kernel(DevPlan P, int node0, T *f
     for (int i = 0; i < nb; ++i)
         if (lane < i) F[(size_t)i * f + lane] = X[i][lane];
     __syncwarp();
-    // upper: x_i = ([i == j] - sum_{t > i} U_it x_t) / U_ii
+    // upper: x_i = ([i == j] - sum_{t > i} U_it x_t) / U_ii, one division per
+    // row (lane i) instead of one per row and lane
+    __shared__ T rdiag[IB];
+    rdiag[lane] = lane < nb ? T(1) / D[lane][lane] : T(1);
+    __syncwarp();
     for (int i = IB - 1; i >= 0; --i) {
         T s = i == lane ? T(1) : T(0);
         for (int t = i + 1; t < IB; ++t) s -= D[i][t] * X[t][lane];
-        const T d = i < nb ? D[i][i] : T(1);
-        X[i][lane] = s / d;
+        X[i][lane] = s * rdiag[i];
     }
     __syncwarp();
     for (int i = 0; i < nb; ++i)
@@ -275,6 +278,7 @@ __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0
     const int c0 = FWD ? 0 : r, c1 = FWD ? r : n;
     T s0 = T(0), s1 = T(0);
     int c = c0 + lane;
+#pragma unroll 4
     for (; c + 32 < c1; c += 64) {
         s0 += row[c] * (T)sv[c];
         s1 += row[c + 32] * (T)sv[c + 32];
@@ -317,6 +321,7 @@ __global__ void __launch_bounds__(VT) inv_apply_rows_kernel(DevPlan P, int node0
     const int c0 = FWD ? 0 : r, c1 = FWD ? r : n;
     T s0 = T(0), s1 = T(0);
     int c = c0;
+    #pragma unroll 4
     for (; c + 2 <= c1; c += 2) {
         s0 += row[c] * (T)sv[c];
         s1 += row[c + 1] * (T)sv[c + 1];

@@ -38,6 +38,8 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       fronts with at most this many 32x32 factor tiles per
                       sweep run as one task (default 48); target tiles per task
                       of the other fronts (default 24)
+  'Leaf Cells'        grid cells of a box at which nested dissection stops
+                      splitting (default 48)
   'CUDA Graphs'       replay the factorisation and solve launch sequences from
                       captured CUDA graphs (default True)
   'Fuse Jacobian'     compute the Jacobian together with the RHS and reuse it
@@ -137,7 +139,8 @@ class Interface:
                              inverse=opts.get('Inverse Apply', True),
                              flow=opts.get('Dataflow Apply', False),
                              flow_fuse_tiles=int(opts.get('Dataflow Fuse Tiles', 48)),
-                             flow_chunk_tiles=int(opts.get('Dataflow Chunk Tiles', 24)))
+                             flow_chunk_tiles=int(opts.get('Dataflow Chunk Tiles', 24)),
+                             leaf_cells=int(opts.get('Leaf Cells', 48)))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

@@ -295,8 +295,10 @@ class Solver:
 
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
                  reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True, flow=False,
-                 flow_fuse_tiles=48, flow_chunk_tiles=24):
+                 flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48):
         self.itf = interface
+        # grid cells at which nested dissection stops splitting a box
+        self.leaf_cells = leaf_cells
         self.inverse = inverse
         # dataflow application (one launch for both sweeps) of the inverted factors
         self.flow = flow and inverse
@@ -343,11 +345,11 @@ class Solver:
         if self.plan is None:
             itf = self.itf
             pvar = itf.dim if itf.dof > itf.dim else None
-            key = (itf.nx, itf.ny, itf.nz, itf.dim, itf.dof, pvar, str(pattern.rowptr.device))
+            key = (itf.nx, itf.ny, itf.nz, itf.dim, itf.dof, pvar, self.leaf_cells, str(pattern.rowptr.device))
             with _PLANS_LOCK:
                 plan = _PLANS.get(key)
                 if plan is None:
-                    plan = NdPlanDevice(pattern, itf.nx, itf.ny, itf.nz, itf.dof, pvar)
+                    plan = NdPlanDevice(pattern, itf.nx, itf.ny, itf.nz, itf.dof, pvar, leaf_cells=self.leaf_cells)
                     # the uploads ran on this thread's stream: finish them
                     # before another thread's stream can read the plan
                     torch.cuda.current_stream().synchronize()
