@@ -276,6 +276,17 @@ int tf_nd_invert_f64(const tf_nd_plan *plan, double *d_fronts, double *d_work, s
                      tf_stream_t stream);
 int tf_nd_invert_f32(const tf_nd_plan *plan, float *d_fronts, float *d_work, size_t work_bytes,
                      tf_stream_t stream);
+/* tf_nd_factor_* followed by tf_nd_invert_*, with the inversion of each tree
+ * height's own blocks on aux_stream as soon as that height is factored, so
+ * that it overlaps the factorisation of the heights above.  aux_stream must
+ * differ from stream and is joined back into stream before the call returns
+ * (also inside a stream capture: the pair becomes one graph).               */
+int tf_nd_factor_inv_f64(const tf_nd_plan *plan, const double *d_vals, double *d_fronts, int32_t *d_piv,
+                         int32_t *d_info, double *d_work, size_t work_bytes, tf_stream_t stream,
+                         tf_stream_t aux_stream);
+int tf_nd_factor_inv_f32(const tf_nd_plan *plan, const double *d_vals, float *d_fronts, int32_t *d_piv,
+                         int32_t *d_info, float *d_work, size_t work_bytes, tf_stream_t stream,
+                         tf_stream_t aux_stream);
 /* In-place solve with inverted own blocks (after tf_nd_invert_*): d_x as in
  * tf_nd_solve_*; d_scratch: tf_nd_solve_inv_workspace_bytes(plan) bytes of
  * device scratch (one value per front index entry; the query reads the

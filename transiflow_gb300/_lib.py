@@ -129,6 +129,8 @@ _SIGNATURES = {
     'tf_nd_invert_workspace_bytes': ([_P, _I], ctypes.c_size_t),
     'tf_nd_invert_f64': ([_P, _P, _P, ctypes.c_size_t, _P], _I),
     'tf_nd_invert_f32': ([_P, _P, _P, ctypes.c_size_t, _P], _I),
+    'tf_nd_factor_inv_f64': ([_P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P, _P], _I),
+    'tf_nd_factor_inv_f32': ([_P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P, _P], _I),
     'tf_nd_solve_inv_workspace_bytes': ([_P], ctypes.c_size_t),
     'tf_nd_solve_inv_f64': ([_P, _P, _P, _P, _P, _P], _I),
     'tf_nd_solve_inv_f32': ([_P, _P, _P, _P, _P, _P], _I),

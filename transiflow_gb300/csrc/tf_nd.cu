@@ -490,8 +490,8 @@ int ensure_smem(const void *kernel, size_t bytes) {
 }
 
 template <typename T>
-static int factor(const tf_nd_plan *p, const double *vals, T *fronts, int32_t *piv, int32_t *info,
-                  cudaStream_t s) {
+int factor(const tf_nd_plan *p, const double *vals, T *fronts, int32_t *piv, int32_t *info, cudaStream_t s,
+           const std::function<int(int)> *after_level) {
     int e = check_plan(p);
     if (e) return e;
     if (!vals || !fronts || !piv) return TF_ERR_ARG;
@@ -539,6 +539,7 @@ static int factor(const tf_nd_plan *p, const double *vals, T *fronts, int32_t *p
             dim3 ge(64, cnt);
             extend_add_kernel<T><<<ge, 256, 0, s>>>(D, node0, rank, fronts); launched();
         }
+        if (after_level && (e = (*after_level)(h))) return e;
     }
     pivots_to_permutation_kernel<<<p->nnodes, 256, perm_smem, s>>>(D, p->nnodes, piv);
     launched();
@@ -610,6 +611,10 @@ static int solve(const tf_nd_plan *p, const T *fronts, const int32_t *piv, doubl
     return cuda_status();
 }
 
+template int factor<float>(const tf_nd_plan *, const double *, float *, int32_t *, int32_t *, cudaStream_t,
+                           const std::function<int(int)> *);
+template int factor<double>(const tf_nd_plan *, const double *, double *, int32_t *, int32_t *, cudaStream_t,
+                            const std::function<int(int)> *);
 template void bnd<float, true>(const DevPlan &, int, int, int, int, const float *, double *, cudaStream_t);
 template void bnd<float, false>(const DevPlan &, int, int, int, int, const float *, double *, cudaStream_t);
 template void bnd<double, true>(const DevPlan &, int, int, int, int, const double *, double *, cudaStream_t);
@@ -622,12 +627,12 @@ using namespace tf;
 
 extern "C" int tf_nd_factor_f64(const tf_nd_plan *plan, const double *d_vals, double *d_fronts, int32_t *d_piv,
                                 int32_t *d_info, tf_stream_t stream) {
-    return nd::factor<double>(plan, d_vals, d_fronts, d_piv, d_info, (cudaStream_t)stream);
+    return nd::factor<double>(plan, d_vals, d_fronts, d_piv, d_info, (cudaStream_t)stream, nullptr);
 }
 
 extern "C" int tf_nd_factor_f32(const tf_nd_plan *plan, const double *d_vals, float *d_fronts, int32_t *d_piv,
                                 int32_t *d_info, tf_stream_t stream) {
-    return nd::factor<float>(plan, d_vals, d_fronts, d_piv, d_info, (cudaStream_t)stream);
+    return nd::factor<float>(plan, d_vals, d_fronts, d_piv, d_info, (cudaStream_t)stream, nullptr);
 }
 
 extern "C" int tf_nd_solve_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_t *d_piv, double *d_x,

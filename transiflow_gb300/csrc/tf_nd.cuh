@@ -8,6 +8,8 @@
 
 #include <cooperative_groups.h>
 
+#include <functional>
+
 namespace tf {
 namespace nd {
 
@@ -76,6 +78,13 @@ int ensure_smem(const void *kernel, size_t bytes);
 
 DevPlan dev_plan(const tf_nd_plan *p, const int32_t *rank);
 int check_plan(const tf_nd_plan *p);
+
+// Numeric factorisation of every front, height by height on stream s; after
+// each height (its fronts factored and their Schur complements added into the
+// parents) `after_level(h)`, when given, may enqueue work that depends on it.
+template <typename T>
+int factor(const tf_nd_plan *p, const double *vals, T *fronts, int32_t *piv, int32_t *info, cudaStream_t s,
+           const std::function<int(int)> *after_level);
 
 // x[bnd] -= L21 y (FWD) or x[own] -= U12 x[bnd] for every front of one tree
 // height (rows x cols at most per front).

@@ -24,6 +24,7 @@
 #include "tf_nd.cuh"
 
 #include <algorithm>
+#include <vector>
 
 namespace tf {
 namespace nd {
@@ -208,34 +209,72 @@ static size_t invert_work_elems(const tf_nd_plan *p) {
     return w;
 }
 
+// Inversion of the own blocks of the fronts of height h (scratch `work` of
+// invert_work_elems elements, reused by every height).
+template <typename T>
+static void invert_level(const tf_nd_plan *p, const DevPlan &D, int h, T *fronts, T *work, cudaStream_t s) {
+    const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
+    const int mo = p->max_own[h];
+    if (cnt <= 0 || mo <= 0) return;
+    inv_diag_kernel<T><<<dim3((mo + IB - 1) / IB, cnt), 32, 0, s>>>(D, node0, fronts);
+    launched();
+    const int ld = inv_ld(mo);
+    const int64_t stride = (int64_t)mo * ld;
+    for (int depth = inv_depths(mo) - 1; depth >= 0; --depth) {
+        // the largest node at this depth has at most split_at(mo >> depth)-ish rows; bound the
+        // tile grid by the root's halves
+        const int half = split_at(mo);
+        const int tiles = ((half + IT - 1) / IT) * ((half + IT - 1) / IT);
+        dim3 g(tiles, 1 << depth, cnt);
+        inv_gemm_kernel<T, false, 0><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+        launched();
+        inv_gemm_kernel<T, false, 1><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+        launched();
+        inv_gemm_kernel<T, true, 0><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+        launched();
+        inv_gemm_kernel<T, true, 1><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+        launched();
+    }
+}
+
 template <typename T>
 static int invert(const tf_nd_plan *p, const DevPlan &D, T *fronts, T *work, size_t work_bytes, cudaStream_t s) {
     if (work_bytes < invert_work_elems(p) * sizeof(T)) return TF_ERR_ARG;
-    for (int h = 0; h < p->nlevels; ++h) {
-        const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
-        const int mo = p->max_own[h];
-        if (cnt <= 0 || mo <= 0) continue;
-        inv_diag_kernel<T><<<dim3((mo + IB - 1) / IB, cnt), 32, 0, s>>>(D, node0, fronts);
-        launched();
-        const int ld = inv_ld(mo);
-        const int64_t stride = (int64_t)mo * ld;
-        for (int depth = inv_depths(mo) - 1; depth >= 0; --depth) {
-            // the largest node at this depth has at most split_at(mo >> depth)-ish rows; bound the
-            // tile grid by the root's halves
-            const int half = split_at(mo);
-            const int tiles = ((half + IT - 1) / IT) * ((half + IT - 1) / IT);
-            dim3 g(tiles, 1 << depth, cnt);
-            inv_gemm_kernel<T, false, 0><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
-            launched();
-            inv_gemm_kernel<T, false, 1><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
-            launched();
-            inv_gemm_kernel<T, true, 0><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
-            launched();
-            inv_gemm_kernel<T, true, 1><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
-            launched();
-        }
-    }
+    for (int h = 0; h < p->nlevels; ++h) invert_level<T>(p, D, h, fronts, work, s);
     return cuda_status();
+}
+
+// Factorisation on stream s with the inversion of each height's own blocks on
+// stream aux as soon as that height is factored: the inversions (small,
+// latency-bound launches) overlap the factorisation of the heights above,
+// which near the root leaves most SMs idle.  The inversion of height h
+// touches only the own blocks of height h, which nothing later in the
+// factorisation reads.  aux joins s again before the return, also inside a
+// stream capture.
+template <typename T>
+static int factor_invert(const tf_nd_plan *p, const double *vals, T *fronts, int32_t *piv, int32_t *info, T *work,
+                         size_t work_bytes, cudaStream_t s, cudaStream_t aux) {
+    if (work_bytes < invert_work_elems(p) * sizeof(T)) return TF_ERR_ARG;
+    const DevPlan D = dev_plan(p, p->d_rank);
+    std::vector<cudaEvent_t> ev(p->nlevels + 1, nullptr);
+    int e = TF_OK;
+    for (auto &x : ev)
+        if (cudaEventCreateWithFlags(&x, cudaEventDisableTiming) != cudaSuccess) e = TF_ERR_CUDA;
+    if (!e) {
+        const std::function<int(int)> hook = [&](int h) -> int {
+            if (cudaEventRecord(ev[h], s) != cudaSuccess || cudaStreamWaitEvent(aux, ev[h], 0) != cudaSuccess)
+                return TF_ERR_CUDA;
+            invert_level<T>(p, D, h, fronts, work, aux);
+            return TF_OK;
+        };
+        e = factor<T>(p, vals, fronts, piv, info, s, &hook);
+        if (cudaEventRecord(ev[p->nlevels], aux) != cudaSuccess ||
+            cudaStreamWaitEvent(s, ev[p->nlevels], 0) != cudaSuccess)
+            e = e ? e : TF_ERR_CUDA;
+    }
+    for (auto &x : ev)
+        if (x) cudaEventDestroy(x);
+    return e ? e : cuda_status();
 }
 
 // ---------------------------------------------------------------------------
@@ -462,6 +501,30 @@ extern "C" size_t tf_nd_solve_inv_workspace_bytes(const tf_nd_plan *plan) {
         return 0;
     }
     return (size_t)len * sizeof(double);
+}
+
+extern "C" int tf_nd_factor_inv_f64(const tf_nd_plan *plan, const double *d_vals, double *d_fronts, int32_t *d_piv,
+                                    int32_t *d_info, double *d_work, size_t work_bytes, tf_stream_t stream,
+                                    tf_stream_t aux_stream) {
+    int e = nd::check_plan(plan);
+    if (e) return e;
+    if (!d_vals || !d_fronts || !d_piv || !aux_stream || aux_stream == stream ||
+        (!d_work && nd::invert_work_elems(plan)))
+        return TF_ERR_ARG;
+    return nd::factor_invert<double>(plan, d_vals, d_fronts, d_piv, d_info, d_work, work_bytes, (cudaStream_t)stream,
+                                     (cudaStream_t)aux_stream);
+}
+
+extern "C" int tf_nd_factor_inv_f32(const tf_nd_plan *plan, const double *d_vals, float *d_fronts, int32_t *d_piv,
+                                    int32_t *d_info, float *d_work, size_t work_bytes, tf_stream_t stream,
+                                    tf_stream_t aux_stream) {
+    int e = nd::check_plan(plan);
+    if (e) return e;
+    if (!d_vals || !d_fronts || !d_piv || !aux_stream || aux_stream == stream ||
+        (!d_work && nd::invert_work_elems(plan)))
+        return TF_ERR_ARG;
+    return nd::factor_invert<float>(plan, d_vals, d_fronts, d_piv, d_info, d_work, work_bytes, (cudaStream_t)stream,
+                                    (cudaStream_t)aux_stream);
 }
 
 extern "C" int tf_nd_invert_f64(const tf_nd_plan *plan, double *d_fronts, double *d_work, size_t work_bytes,

@@ -15,6 +15,7 @@ gauge entry is zeroed (SciPy.py:211-216), and a bordered system
 with two solves of the gauged Jacobian.
 """
 
+import ctypes
 import math
 import threading
 
@@ -252,11 +253,15 @@ class _Engine:
                     _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(),
                                       self.scratch.data_ptr(), _stream()), 'tf_nd_solve_inv')
 
+            # the inversion of each height overlaps the factorisation of the
+            # heights above it on a second stream
+            self.aux = torch.cuda.Stream(device=dev)
+            facinv_fn = lib.tf_nd_factor_inv_f64 if f64 else lib.tf_nd_factor_inv_f32
+
             def factor():
-                _lib.check(fac_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
-                                  info.data_ptr(), _stream()), 'tf_nd_factor')
-                _lib.check(inv_fn(sp, fronts.data_ptr(), self.work.data_ptr(), wbytes, _stream()),
-                           'tf_nd_invert')
+                _lib.check(facinv_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
+                                     info.data_ptr(), self.work.data_ptr(), wbytes, _stream(),
+                                     ctypes.c_void_p(self.aux.cuda_stream)), 'tf_nd_factor_inv')
         else:
             self.flow = None
             sol_fn = lib.tf_nd_solve_f64 if f64 else lib.tf_nd_solve_f32
