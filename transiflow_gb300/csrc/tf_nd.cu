@@ -33,7 +33,7 @@ constexpr int TRSM_THREADS = 64;
 
 // Boundary rows [n, f) of the panel: X = F[r, k:k+nb] U_pp^-1
 template <typename T>
-__global__ void __launch_bounds__(TRSM_THREADS) lower_kernel(DevPlan P, int node0, int k, T *fronts) {
+__device__ __forceinline__ void lower_rows(const DevPlan &P, int node0, int k, T *fronts) {
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
     if (k >= n) return;
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(TRSM_THREADS) lower_kernel(DevPlan P, int node
 
 // Block row to the right of the panel: X = L_pp^-1 F[k:k+nb, j], j >= k+nb
 template <typename T>
-__global__ void __launch_bounds__(TRSM_THREADS) urow_kernel(DevPlan P, int node0, int k, T *fronts) {
+__device__ __forceinline__ void urow_cols(const DevPlan &P, int node0, int k, T *fronts) {
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
     if (k >= n) return;
@@ -99,6 +99,14 @@ __global__ void __launch_bounds__(TRSM_THREADS) urow_kernel(DevPlan P, int node0
 #pragma unroll
     for (int c = 0; c < NB; ++c)
         if (c < nb) F[(size_t)(k + c) * f + j] = x[c];
+}
+
+// Both triangular solves of one panel step in one launch (grid.z = 0: the
+// boundary rows, 1: the block row); they are independent of each other.
+template <typename T>
+__global__ void __launch_bounds__(TRSM_THREADS) trsm_kernel(DevPlan P, int node0, int k, T *fronts) {
+    if (blockIdx.z == 0) lower_rows(P, node0, k, fronts);
+    else urow_cols(P, node0, k, fronts);
 }
 
 // Trailing update F[r][j] -= sum_q F[r][k+q] F[k+q][j], r, j >= k+nb
@@ -517,9 +525,8 @@ int factor(const tf_nd_plan *p, const double *vals, T *fronts, int32_t *piv, int
             if ((e = panel<T>(D, node0, cnt, k, mo - k, nsm, fronts, piv, info, s))) return e;
             const int rest = mf - k - 1;
             if (mf > 0) {
-                dim3 gl((mf + TRSM_THREADS - 1) / TRSM_THREADS, cnt);
-                lower_kernel<T><<<gl, TRSM_THREADS, 0, s>>>(D, node0, k, fronts); launched();
-                urow_kernel<T><<<gl, TRSM_THREADS, 0, s>>>(D, node0, k, fronts); launched();
+                dim3 gl((mf + TRSM_THREADS - 1) / TRSM_THREADS, cnt, 2);
+                trsm_kernel<T><<<gl, TRSM_THREADS, 0, s>>>(D, node0, k, fronts); launched();
             }
             if (rest > 0) {
                 if constexpr (sizeof(T) == 4) {
