@@ -62,7 +62,7 @@ def parse():
                     help='time this many random lid-driven cavities (nx from 32..192, Re from [100, 4000], '
                          'seed 2) solved concurrently and one after the other, then exit')
     ap.add_argument('--re', type=float, default=1000.0, help='Reynolds number of the --profile state')
-    ap.add_argument('--apply', default='levels', choices=['flow', 'levels'],
+    ap.add_argument('--apply', default='levels', choices=['flow', 'levels', 'sweep'],
                     help='application of the inverted factors: one dataflow launch or one launch per tree height')
     ap.add_argument('--flow-fuse', type=int, default=48, help='dataflow apply: most factor tiles of a warp-task front')
     ap.add_argument('--flow-chunk', type=int, default=24, help='dataflow apply: target tiles per CTA task')
@@ -157,7 +157,8 @@ def gpu_arm(args, rank, world, local):
     torch.cuda.set_device(local)
     lib = _lib.load()
     params = {'CUDA': {'Factor Precision': args.precision, 'Tolerance': args.tol,
-                       'Dataflow Apply': args.apply == 'flow', 'Dataflow Fuse Tiles': args.flow_fuse,
+                       'Dataflow Apply': args.apply == 'flow', 'Sweep Apply': args.apply == 'sweep',
+                       'Dataflow Fuse Tiles': args.flow_fuse,
                        'Dataflow Chunk Tiles': args.flow_chunk, 'Leaf Cells': args.leaf_cells}}
     itf = Interface(params, args.nx, args.nx, args.nz)
     n = itf.n
@@ -440,6 +441,7 @@ def profile_stage(args):
     from transiflow_gb300 import Interface
     p = {'Reynolds Number': args.re, 'CUDA': {'Factor Precision': args.precision, 'CUDA Graphs': False,
                                               'Dataflow Apply': args.apply == 'flow',
+                                              'Sweep Apply': args.apply == 'sweep',
                                               'Dataflow Fuse Tiles': args.flow_fuse,
                                               'Dataflow Chunk Tiles': args.flow_chunk, 'Leaf Cells': args.leaf_cells}}
     itf = Interface(p, args.nx, args.nx, args.nz)

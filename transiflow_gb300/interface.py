@@ -34,6 +34,9 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       for the fronts it depends on (default False; plans whose
                       widest front does not fit that launch's shared memory
                       keep one launch per tree height)
+  'Sweep Apply'       with 'Inverse Apply': both sweeps in one cooperative
+                      launch, the tree heights separated by grid-wide barriers
+                      (default False)
   'Dataflow Fuse Tiles', 'Dataflow Chunk Tiles'
                       fronts with at most this many 32x32 factor tiles per
                       sweep run as one task (default 48); target tiles per task
@@ -140,7 +143,8 @@ class Interface:
                              flow=opts.get('Dataflow Apply', False),
                              flow_fuse_tiles=int(opts.get('Dataflow Fuse Tiles', 48)),
                              flow_chunk_tiles=int(opts.get('Dataflow Chunk Tiles', 24)),
-                             leaf_cells=int(opts.get('Leaf Cells', 48)))
+                             leaf_cells=int(opts.get('Leaf Cells', 48)),
+                             sweep=opts.get('Sweep Apply', False))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

@@ -226,7 +226,15 @@ class _Engine:
             wbytes = lib.tf_nd_invert_workspace_bytes(sp, 8 if f64 else 4)
             self.work = torch.empty(max(1, (wbytes + 7) // 8), dtype=torch.float64, device=dev)
             self.flow = None
-            if solver.flow:
+            self.sweep = None
+            if solver.sweep:
+                # both sweeps in one cooperative launch, heights separated by
+                # grid barriers
+                sw_bytes = lib.tf_nd_sweep_workspace_bytes(sp)
+                # zero-filled: its first word is the sticky error word
+                self.sweep = torch.zeros((sw_bytes + 7) // 8, dtype=torch.float64, device=dev)
+                sweep_fn = lib.tf_nd_solve_sweep_f64 if f64 else lib.tf_nd_solve_sweep_f32
+            elif solver.flow:
                 # both sweeps in one persistent launch (dataflow over the
                 # elimination tree); plans whose widest front does not fit
                 # the launch's shared memory keep the per-height launches
@@ -239,7 +247,13 @@ class _Engine:
                         self.flow = flow
                     elif code != 4:     # TF_ERR_SIZE: fall back to the per-height launches
                         _lib.check(code, 'tf_nd_flow_prepare')
-            if self.flow is not None:
+            if self.sweep is not None:
+
+                def solve():
+                    _lib.check(sweep_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(),
+                                        self.sweep.data_ptr(), self.sweep.numel() * 8, _stream()),
+                               'tf_nd_solve_sweep')
+            elif self.flow is not None:
                 flow_fn = lib.tf_nd_solve_flow_f64 if f64 else lib.tf_nd_solve_flow_f32
 
                 def solve():
@@ -264,6 +278,7 @@ class _Engine:
                                      ctypes.c_void_p(self.aux.cuda_stream)), 'tf_nd_factor_inv')
         else:
             self.flow = None
+            self.sweep = None
             sol_fn = lib.tf_nd_solve_f64 if f64 else lib.tf_nd_solve_f32
 
             def factor():
@@ -288,6 +303,8 @@ class _Engine:
         since the last check (synchronising)."""
         if self.flow is not None:
             _lib.check(self.lib.tf_nd_flow_status(self.flow.data_ptr()), 'tf_nd_solve_flow')
+        if self.sweep is not None:
+            _lib.check(self.lib.tf_nd_sweep_status(self.sweep.data_ptr()), 'tf_nd_solve_sweep')
 
 
 def _struct_ptr(s):
@@ -300,13 +317,15 @@ class Solver:
 
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
                  reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True, flow=False,
-                 flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48):
+                 flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48, sweep=False):
         self.itf = interface
         # grid cells at which nested dissection stops splitting a box
         self.leaf_cells = leaf_cells
         self.inverse = inverse
         # dataflow application (one launch for both sweeps) of the inverted factors
         self.flow = flow and inverse
+        # cooperative one-launch application, heights separated by grid barriers
+        self.sweep = sweep and inverse
         self.flow_fuse_tiles = flow_fuse_tiles
         self.flow_chunk_tiles = flow_chunk_tiles
         self.graphs = graphs
