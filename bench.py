@@ -264,9 +264,10 @@ def fp64_peak():
     return 2.0 * 4096 ** 3 / best / 1e12
 
 
-# DRAM bytes (read + write) of one factorisation, summed over its launches in
-# one ncu capture of `bench.py --profile factor` on a GB300.
-FACTOR_TRAFFIC = {(256, 1, 'fp64'): 6.046e9}
+# DRAM bytes (read + write) of one factorisation with the inversion of its own
+# blocks, summed over its launches in one ncu capture of
+# `bench.py --profile factor` on a GB300.
+FACTOR_TRAFFIC = {(256, 1, 'fp64'): 6.353e9}
 
 
 def roofline(itf, x, args, lib):

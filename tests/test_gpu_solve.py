@@ -181,3 +181,49 @@ def test_sweep_application_in_graphed_gmres(precision):
     bg[itf.dim] = 0
     assert np.linalg.norm(A @ y - bg) / np.linalg.norm(bg) < 1e-11
     assert itf.solver._engine(precision).sweep is not None
+
+
+def test_dataflow_wait_times_out_and_reports():
+    """Failure detection of the bounded waits: one task of the dataflow
+    application is made to wait for a counter value that no task produces.
+    Its wait gives up after its poll limit (about a second), the others
+    return through the abort word, tf_nd_flow_status reports TF_ERR_TIMEOUT
+    once, and the context stays usable: re-preparing the task list gives the
+    correct application again."""
+    import ctypes
+    import torch
+    from transiflow_gb300 import Interface, _lib
+    p = {'Reynolds Number': 500, 'CUDA': {'CUDA Graphs': False, 'Dataflow Apply': True,
+                                          'Dataflow Fuse Tiles': 0, 'Dataflow Chunk Tiles': 8}}
+    itf = Interface(p, 24, 24)
+    rng = np.random.default_rng(11)
+    J = itf.jacobian(itf.vector_from_array(0.3 * rng.standard_normal(itf.n)))
+    fac = itf.solver.factorization(J)
+    eng = itf.solver._engine('fp64')
+    b = rng.standard_normal(itf.n)
+    b[itf.dim] = 0.0
+    good = torch.as_tensor(b.copy()).to(itf.device)
+    fac.apply(good)
+    eng.check()
+    # header: err, ntasks, pad, pad (int32), then tasks_off (int64, bytes 16-23);
+    # task: node, kind, r0, r1, wait, target, signal, pad (int32)
+    words = eng.flow.view(torch.int32)
+    ntasks = int(words[1])
+    tasks_off = int(eng.flow.view(torch.int64)[2])
+    assert tasks_off % 32 == 0 and tasks_off >= 56
+    tasks = words[tasks_off // 4: tasks_off // 4 + 8 * ntasks].view(ntasks, 8)
+    waiting = torch.nonzero(tasks[:, 5] > 0).flatten()
+    assert len(waiting) > 0
+    k = int(waiting[len(waiting) // 2])
+    tasks[k, 5] += 1                      # a count no task reaches
+    bad = torch.as_tensor(b.copy()).to(itf.device)
+    fac.apply(bad)
+    torch.cuda.synchronize()
+    lib = _lib.load()
+    assert lib.tf_nd_flow_status(ctypes.c_void_p(eng.flow.data_ptr())) == 5     # TF_ERR_TIMEOUT
+    assert lib.tf_nd_flow_status(ctypes.c_void_p(eng.flow.data_ptr())) == 0     # sticky word cleared
+    tasks[k, 5] -= 1
+    again = torch.as_tensor(b.copy()).to(itf.device)
+    fac.apply(again)
+    eng.check()
+    assert torch.allclose(again, good, rtol=1e-12, atol=1e-12 * float(good.abs().max()))
