@@ -210,7 +210,7 @@ def test_dataflow_wait_times_out_and_reports():
     words = eng.flow.view(torch.int32)
     ntasks = int(words[1])
     tasks_off = int(eng.flow.view(torch.int64)[2])
-    assert tasks_off % 32 == 0 and tasks_off >= 56
+    assert tasks_off % 16 == 0 and tasks_off >= 56
     tasks = words[tasks_off // 4: tasks_off // 4 + 8 * ntasks].view(ntasks, 8)
     waiting = torch.nonzero(tasks[:, 5] > 0).flatten()
     assert len(waiting) > 0
