@@ -319,6 +319,17 @@ int tf_nd_solve_flow_f64(const tf_nd_plan *plan, const double *d_fronts, const i
 int tf_nd_solve_flow_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,
                          double *d_x, void *d_work, tf_stream_t stream);
 int tf_nd_flow_status(void *d_work);
+/* Host-only: the task list tf_nd_flow_prepare builds, from host copies of the
+ * plan's per-front own sizes, front sizes and parents and its level_ptr.
+ * tasks: 8 int32 per task (front, kind, first row, end row, counter waited
+ * for or -1, target count, counter signalled or -1, 0); nodes: 8 int32 per
+ * front (forward wait, target, signal, backward wait, target, signal, 0, 0),
+ * read by the one-warp tasks of small fronts (kinds 5 forward, 6 backward,
+ * front range [front, front + first row)).  With tasks or nodes NULL only
+ * *ntasks is set.  No device memory is touched.                             */
+int tf_nd_flow_tasks_host(int nnodes, const int32_t *n_own, const int32_t *f, const int32_t *parent,
+                          int nlevels, const int32_t *level_ptr, int fuse_tiles, int chunk_tiles,
+                          int32_t *tasks, int32_t *nodes, int max_tasks, int *ntasks);
 
 /* The same application as tf_nd_solve_inv_* in ONE cooperative launch: the
  * products of each tree height and sweep are phases separated by grid-wide

@@ -162,3 +162,126 @@ def test_metric_table_matches_oracle_spacings():
     m = fvm._Metric(x, 12)
     assert np.array_equal(t[0, 0, :12], m.D) and np.array_equal(t[0, 3, :12], m.Hp)
     assert np.array_equal(t[0, 8, :12], m.w0) and np.array_equal(t[0, 9, :12], m.w1)
+
+
+K_FOWN, K_FBND, K_BBND, K_BOWN, K_WFWD, K_WBWD = 0, 1, 3, 4, 5, 6
+
+
+def _flow_tasks(lib, plan, fuse, chunk):
+    import ctypes
+    n = np.ascontiguousarray(plan.n_own, dtype=np.int32)
+    f = np.ascontiguousarray(plan.f, dtype=np.int32)
+    par = np.ascontiguousarray(plan.parent, dtype=np.int32)
+    lp = np.cumsum([0] + [len(l) for l in plan.levels]).astype(np.int32)
+    assert (np.concatenate(plan.levels) == np.arange(plan.nnodes)).all()
+    cnt = ctypes.c_int(0)
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    args = (plan.nnodes, ptr(n), ptr(f), ptr(par), len(plan.levels), ptr(lp), fuse, chunk)
+    assert lib.tf_nd_flow_tasks_host(*args, None, None, 0, ctypes.byref(cnt)) == 0
+    tasks = np.zeros((cnt.value, 8), np.int32)
+    nodes = np.zeros((plan.nnodes, 8), np.int32)
+    assert lib.tf_nd_flow_tasks_host(*args, ptr(tasks), ptr(nodes), cnt.value, ctypes.byref(cnt)) == 0
+    return tasks, nodes
+
+
+@pytest.mark.parametrize('fuse,chunk', [(0, 1), (0, 24), (12, 8), (48, 24), (10 ** 6, 24)])
+@pytest.mark.parametrize('case', [({'Reynolds Number': 100}, 32, 24, 1),
+                                  ({'Reynolds Number': 100}, 6, 6, 6)])
+def test_dataflow_task_list_follows_the_elimination_tree(built_lib, case, fuse, chunk):
+    """The task list of the one-launch dataflow application (built by the
+    library's own host code) covers every row of every front once per part of
+    each sweep, every counter is signalled exactly as often as its waiters
+    expect and only by tasks earlier in the list (so the launch cannot
+    deadlock whatever number of CTAs is resident), and the waits imply every
+    dependency of the substitution: descendants before a front's forward,
+    ancestors before its backward."""
+    params, nx, ny, nz = case
+    d = fvm.Discretization(dict(params), nx, ny, nz)
+    A = _gauged(d.jacobian(np.random.default_rng(0).standard_normal(nx * ny * nz * d.dof)).to_scipy(), d.dim)
+    plan = build_plan(nx, ny, nz, d.dof, A.indptr, A.indices, pressure_var=d.dim)
+    T0, NF = _flow_tasks(built_lib, plan, fuse, chunk)
+    n, f, par = plan.n_own, plan.f, plan.parent
+    # expand warp bundles into one pseudo task per front (kinds 100 / 101)
+    rows = []
+    for t in T0:
+        if t[1] in (K_WFWD, K_WBWD):
+            assert 1 <= t[2] <= 8
+            for i in range(t[0], t[0] + t[2]):
+                w, tg, sg = NF[i, 0:3] if t[1] == K_WFWD else NF[i, 3:6]
+                rows.append([i, 100 if t[1] == K_WFWD else 101, 0, 0, w, tg, sg, 0])
+        else:
+            rows.append(list(t))
+    T = np.array(rows, np.int64)
+    cov = {}
+    for node, kind, r0, r1 in T[:, :4]:
+        cov.setdefault((node, kind), []).append((r0, r1))
+    for i in range(plan.nnodes):
+        if (i, 100) in cov:
+            assert len(cov[(i, 100)]) == 1 and len(cov[(i, 101)]) == 1
+            continue
+        for kind, lo, hi in [(K_FOWN, 0, n[i]), (K_FBND, n[i], f[i]), (K_BBND, 0, n[i]), (K_BOWN, 0, n[i])]:
+            rs = sorted(cov.get((i, kind), []))
+            if hi == lo:
+                assert not rs
+                continue
+            assert rs[0][0] == lo and rs[-1][1] == hi
+            assert all(a[1] == b[0] for a, b in zip(rs, rs[1:]))
+    sig = {}
+    for k, t in enumerate(T):
+        if t[6] >= 0:
+            sig.setdefault(int(t[6]), []).append(k)
+    done = [0] * len(T)
+    for k, t in enumerate(T):
+        if t[4] >= 0 and t[5] > 0:
+            s = sig.get(int(t[4]), [])
+            assert len(s) == t[5] and max(s) < k
+            m = 0
+            for j in s:
+                m |= (1 << j) | done[j]
+            done[k] = m
+        else:
+            assert t[5] == 0
+    of = {}
+    for k, t in enumerate(T):
+        of.setdefault((int(t[0]), int(t[1])), []).append(k)
+
+    def mask(fronts, kinds):
+        m = 0
+        for i in fronts:
+            for kd in kinds:
+                for k in of.get((i, kd), []):
+                    m |= 1 << k
+        return m
+
+    kids = [[] for _ in range(plan.nnodes)]
+    for i in range(plan.nnodes):
+        if par[i] >= 0:
+            kids[par[i]].append(i)
+
+    def desc(i):
+        out, st = [], list(kids[i])
+        while st:
+            c = st.pop()
+            out.append(c)
+            st.extend(kids[c])
+        return out
+
+    def anc(i):
+        out, a = [], par[i]
+        while a >= 0:
+            out.append(a)
+            a = par[a]
+        return out
+
+    fw = (K_FOWN, K_FBND, 100)
+    for k, t in enumerate(T):
+        i, kind = int(t[0]), int(t[1])
+        if kind in (K_FOWN, 100):
+            need = mask(desc(i), fw)
+        elif kind == K_FBND:
+            need = mask([i], (K_FOWN,))
+        elif kind in (K_BBND, 101):
+            need = mask(anc(i), (K_BOWN, 101)) | mask([i] + desc(i), fw)
+        else:
+            need = mask([i], (K_BBND,))
+        assert need & ~done[k] == 0

@@ -664,6 +664,30 @@ extern "C" int tf_nd_flow_prepare(const tf_nd_plan *plan, void *d_work, size_t w
     return TF_OK;
 }
 
+extern "C" int tf_nd_flow_tasks_host(int nnodes, const int32_t *n_own, const int32_t *f, const int32_t *parent,
+                                     int nlevels, const int32_t *level_ptr, int fuse_tiles, int chunk_tiles,
+                                     int32_t *tasks, int32_t *nodes, int max_tasks, int *ntasks) {
+    if (nnodes <= 0 || nlevels <= 0 || !n_own || !f || !parent || !level_ptr || !ntasks) return TF_ERR_ARG;
+    nd::FlowPlanHost h;
+    h.n.assign(n_own, n_own + nnodes);
+    h.f.assign(f, f + nnodes);
+    h.parent.assign(parent, parent + nnodes);
+    tf_nd_plan p = {};
+    p.nnodes = nnodes;
+    p.nlevels = nlevels;
+    p.level_ptr = level_ptr;
+    std::vector<nd::FlowTask> t;
+    std::vector<nd::NodeFlow> nf;
+    const int e = nd::flow_build(&p, h, fuse_tiles, chunk_tiles, t, nf);
+    if (e) return e;
+    *ntasks = (int)t.size();
+    if (!tasks || !nodes) return TF_OK;          // size query
+    if ((int)t.size() > max_tasks) return TF_ERR_SIZE;
+    std::copy_n(reinterpret_cast<const int32_t *>(t.data()), 8 * t.size(), tasks);
+    std::copy_n(reinterpret_cast<const int32_t *>(nf.data()), 8 * nf.size(), nodes);
+    return TF_OK;
+}
+
 extern "C" int tf_nd_solve_flow_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_t *d_piv, double *d_x,
                                     void *d_work, tf_stream_t stream) {
     return nd::solve_flow<double>(plan, d_fronts, d_piv, d_x, d_work, (cudaStream_t)stream);
