@@ -133,6 +133,10 @@ const char *tf_error_string(int code);
  * since load or the last reset; host-side counter, no synchronisation.      */
 long long tf_launch_count(void);
 void tf_launch_count_reset(void);
+/* A non-blocking stream owned by the caller (never shared, unlike pooled
+ * streams: concurrent instances capture CUDA graphs on their own streams). */
+int tf_stream_create(tf_stream_t *out);
+int tf_stream_destroy(tf_stream_t stream);
 
 /* ---- stencil CSR ----------------------------------------------------------
  * The Jacobian is stored as a CSR whose rows have a fixed width per

@@ -104,6 +104,8 @@ _SIGNATURES = {
     'tf_error_string': ([_I], ctypes.c_char_p),
     'tf_launch_count': ([], ctypes.c_longlong),
     'tf_launch_count_reset': ([], None),
+    'tf_stream_create': ([_P], _I),
+    'tf_stream_destroy': ([_P], _I),
     'tf_stencil_layout': ([_I, _I, _P, _P], _I),
     'tf_stencil_pattern': ([_P, _P, _P, _P], _I),
     'tf_assemble': ([_P, _P, _P, _P, _P], _I),
@@ -169,6 +171,21 @@ def load():
         fn.restype = res
     _lib = lib
     return lib
+
+
+def new_stream(device=None):
+    """A torch stream over a CUDA stream of its own (tf_stream_create),
+    destroyed when the returned object is garbage collected.  Pooled torch
+    streams repeat after a few dozen allocations, and two threads capturing
+    and launching on one CUDA stream break each other's graph capture."""
+    import torch
+    import weakref
+    lib = load()
+    handle = ctypes.c_void_p()
+    check(lib.tf_stream_create(ctypes.byref(handle)), 'tf_stream_create')
+    stream = torch.cuda.ExternalStream(handle.value, device=device)
+    weakref.finalize(stream, lib.tf_stream_destroy, handle)
+    return stream
 
 
 def exported_symbols():

@@ -18,6 +18,8 @@ import threading
 
 import torch
 
+from . import _lib
+
 from .continuation import Continuation
 from .interface import Interface
 
@@ -69,7 +71,7 @@ def solve_many(specs, concurrency=None):
         with limit:
             try:
                 torch.cuda.set_device(device)
-                results[i] = solve_instance(specs[i], torch.cuda.Stream())
+                results[i] = solve_instance(specs[i], _lib.new_stream())
             except BaseException as e:   # re-raised on the calling thread
                 errors[i] = e
 

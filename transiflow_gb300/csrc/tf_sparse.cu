@@ -262,6 +262,23 @@ std::atomic<long long> tf::g_launches{0};
 extern "C" long long tf_launch_count(void) { return g_launches.load(); }
 extern "C" void tf_launch_count_reset(void) { g_launches.store(0); }
 
+// A stream of its own for one caller (one solver instance, one helper
+// stream): non-blocking with respect to the legacy default stream, and never
+// shared, unlike pooled streams, so a graph capture on it cannot meet another
+// thread's work.
+extern "C" int tf_stream_create(tf_stream_t *out) {
+    if (!out) return TF_ERR_ARG;
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return TF_ERR_CUDA;
+    *out = (tf_stream_t)s;
+    return TF_OK;
+}
+
+extern "C" int tf_stream_destroy(tf_stream_t stream) {
+    if (!stream) return TF_ERR_ARG;
+    return cudaStreamDestroy((cudaStream_t)stream) == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
 static inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
 
 extern "C" int tf_gauge_values(int n, const int32_t *d_rowptr, const int32_t *d_cols, const double *d_vals,

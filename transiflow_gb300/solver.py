@@ -153,7 +153,7 @@ class _Graphed:
         # which fails while another thread's stream is capturing), one
         # capture at a time.
         cur = torch.cuda.current_stream()
-        side = cur if cur != torch.cuda.default_stream() else torch.cuda.Stream()
+        side = cur if cur != torch.cuda.default_stream() else _lib.new_stream(cur.device)
         g = torch.cuda.CUDAGraph()
         with _CAPTURE_LOCK:
             side.wait_stream(cur)
@@ -269,7 +269,7 @@ class _Engine:
 
             # the inversion of each height overlaps the factorisation of the
             # heights above it on a second stream
-            self.aux = torch.cuda.Stream(device=dev)
+            self.aux = _lib.new_stream(dev)
             facinv_fn = lib.tf_nd_factor_inv_f64 if f64 else lib.tf_nd_factor_inv_f32
 
             def factor():
