@@ -67,6 +67,8 @@ def parse():
     ap.add_argument('--flow-fuse', type=int, default=48, help='dataflow apply: most factor tiles of a warp-task front')
     ap.add_argument('--flow-chunk', type=int, default=24, help='dataflow apply: target tiles per CTA task')
     ap.add_argument('--leaf-cells', type=int, default=48, help='grid cells at which nested dissection stops')
+    ap.add_argument('--sweep-heights', type=int, default=0,
+                    help='with --apply sweep: tree heights nearest the root in the cooperative launch (0: all)')
     return ap.parse_args()
 
 
@@ -157,7 +159,7 @@ def gpu_arm(args, rank, world, local):
     torch.cuda.set_device(local)
     lib = _lib.load()
     params = {'CUDA': {'Factor Precision': args.precision, 'Tolerance': args.tol,
-                       'Dataflow Apply': args.apply == 'flow', 'Sweep Apply': args.apply == 'sweep',
+                       'Dataflow Apply': args.apply == 'flow', 'Sweep Apply': (args.sweep_heights or True) if args.apply == 'sweep' else False,
                        'Dataflow Fuse Tiles': args.flow_fuse,
                        'Dataflow Chunk Tiles': args.flow_chunk, 'Leaf Cells': args.leaf_cells}}
     itf = Interface(params, args.nx, args.nx, args.nz)
@@ -442,7 +444,8 @@ def profile_stage(args):
     from transiflow_gb300 import Interface
     p = {'Reynolds Number': args.re, 'CUDA': {'Factor Precision': args.precision, 'CUDA Graphs': False,
                                               'Dataflow Apply': args.apply == 'flow',
-                                              'Sweep Apply': args.apply == 'sweep',
+                                              'Sweep Apply': ((args.sweep_heights or True)
+                                                              if args.apply == 'sweep' else False),
                                               'Dataflow Fuse Tiles': args.flow_fuse,
                                               'Dataflow Chunk Tiles': args.flow_chunk, 'Leaf Cells': args.leaf_cells}}
     itf = Interface(p, args.nx, args.nx, args.nz)

@@ -119,7 +119,8 @@ def test_one_application_of_the_inverted_factors_solves(shape, params):
                                                         'Temperature Forcing': 1.0})])
 def test_dataflow_application_matches_per_height_launches(shape, params, precision):
     """The one-launch applications of the inverted factors (dataflow over the
-    tree, and cooperative with grid barriers) give the per-height
+    tree, and cooperative with grid barriers, for every height or for the
+    heights nearest the root only) give the per-height
     application's result (up to the order of the sums) -- the dataflow one for
     every split of the fronts into tasks: all split into single strips, the
     defaults, all fused -- and their bounded waits report no time-out."""
@@ -129,10 +130,11 @@ def test_dataflow_application_matches_per_height_launches(shape, params, precisi
     b = None
     results = {}
     for flow, fuse, chunk in [(False, 48, 24), (True, 0, 1), (True, 0, 24), (True, 48, 24), (True, 10 ** 6, 24),
-                              ('sweep', 0, 0)]:
+                              ('sweep', 0, 0), ('sweep', 2, 0), ('sweep', 4, 0)]:
         p = dict(params)
         p['CUDA'] = {'Factor Precision': precision, 'CUDA Graphs': False, 'Dataflow Apply': flow is True,
-                     'Sweep Apply': flow == 'sweep', 'Dataflow Fuse Tiles': fuse, 'Dataflow Chunk Tiles': chunk}
+                     'Sweep Apply': (fuse or True) if flow == 'sweep' else False,
+                     'Dataflow Fuse Tiles': fuse, 'Dataflow Chunk Tiles': chunk}
         itf = Interface(p, nx, ny, nz)
         st = 0.3 * np.random.default_rng(4).standard_normal(itf.n)
         J = itf.jacobian(itf.vector_from_array(st))

@@ -144,8 +144,8 @@ _SIGNATURES = {
     'tf_nd_flow_status': ([_P], _I),
     'tf_nd_flow_tasks_host': ([_I, _P, _P, _P, _I, _P, _I, _I, _P, _P, _I, _P], _I),
     'tf_nd_sweep_workspace_bytes': ([_P], ctypes.c_size_t),
-    'tf_nd_solve_sweep_f64': ([_P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
-    'tf_nd_solve_sweep_f32': ([_P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    'tf_nd_solve_sweep_f64': ([_P, _P, _P, _P, _P, ctypes.c_size_t, _I, _P], _I),
+    'tf_nd_solve_sweep_f32': ([_P, _P, _P, _P, _P, ctypes.c_size_t, _I, _P], _I),
     'tf_nd_sweep_status': ([_P], _I),
 }
 

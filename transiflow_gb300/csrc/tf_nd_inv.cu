@@ -460,28 +460,40 @@ static void inv_bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, in
 }
 
 template <typename T>
-static int solve_inv(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int32_t *piv, double *x,
-                     double *packed, cudaStream_t s) {
+int inv_levels(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int32_t *piv, double *x, double *packed,
+               int h_end, bool fwd, cudaStream_t s) {
     int dev = 0, nsm = 0, e = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return TF_ERR_CUDA;
-    for (int h = 0; h < p->nlevels; ++h) {
+    h_end = std::min(h_end, p->nlevels);
+    for (int i = 0; i < h_end; ++i) {
+        const int h = fwd ? i : h_end - 1 - i;
         const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
         const int mo = p->max_own[h], mf = p->max_f[h];
         if (cnt <= 0 || mo <= 0) continue;
-        if ((e = inv_apply<T, true>(D, node0, cnt, mo, fronts, piv, x, packed, s))) return e;
-        inv_bnd<T, true>(D, node0, cnt, mf, mo, nsm, fronts, x, packed, s);
-    }
-    for (int h = p->nlevels - 1; h >= 0; --h) {
-        const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
-        const int mo = p->max_own[h], mf = p->max_f[h];
-        if (cnt <= 0 || mo <= 0) continue;
-        inv_bnd<T, false>(D, node0, cnt, mo, mf, nsm, fronts, x, packed, s);
-        if ((e = inv_apply<T, false>(D, node0, cnt, mo, fronts, piv, x, packed, s))) return e;
+        if (fwd) {
+            if ((e = inv_apply<T, true>(D, node0, cnt, mo, fronts, piv, x, packed, s))) return e;
+            inv_bnd<T, true>(D, node0, cnt, mf, mo, nsm, fronts, x, packed, s);
+        } else {
+            inv_bnd<T, false>(D, node0, cnt, mo, mf, nsm, fronts, x, packed, s);
+            if ((e = inv_apply<T, false>(D, node0, cnt, mo, fronts, piv, x, packed, s))) return e;
+        }
     }
     return cuda_status();
 }
+
+template <typename T>
+static int solve_inv(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int32_t *piv, double *x,
+                     double *packed, cudaStream_t s) {
+    int e = inv_levels<T>(p, D, fronts, piv, x, packed, p->nlevels, true, s);
+    return e ? e : inv_levels<T>(p, D, fronts, piv, x, packed, p->nlevels, false, s);
+}
+
+template int inv_levels<float>(const tf_nd_plan *, const DevPlan &, const float *, const int32_t *, double *, double *,
+                               int, bool, cudaStream_t);
+template int inv_levels<double>(const tf_nd_plan *, const DevPlan &, const double *, const int32_t *, double *,
+                                double *, int, bool, cudaStream_t);
 
 }  // namespace nd
 }  // namespace tf

@@ -222,23 +222,29 @@ static size_t sweep_smem(int elem) {
     return (size_t)elem * (2 * SW_WARPS * TILE + SW_WARPS * 2 * SB);
 }
 
+// Heights h0 .. nlevels-1 go to the cooperative launch; the heights below
+// (many fronts each, throughput-bound) keep their per-height launches
+// before (forward) and after (backward) it.  top_heights <= 0 or >=
+// nlevels: every height in the cooperative launch.
 template <typename T>
 static int solve_sweep(const tf_nd_plan *p, const T *fronts, const int32_t *piv, double *x, void *work,
-                       size_t work_bytes, cudaStream_t s) {
+                       size_t work_bytes, int top_heights, cudaStream_t s) {
     int e = check_plan(p);
     if (e) return e;
     if (!fronts || !piv || !x || !work || work_bytes < 16) return TF_ERR_ARG;
-    if (p->nlevels > SW_MAX_LEVELS) return TF_ERR_SIZE;
+    const int h0 = top_heights <= 0 || top_heights >= p->nlevels ? 0 : p->nlevels - top_heights;
+    if (p->nlevels - h0 > SW_MAX_LEVELS) return TF_ERR_SIZE;
     SweepArgs A;
-    A.nlevels = p->nlevels;
-    for (int h = 0; h < p->nlevels; ++h) {
+    A.nlevels = p->nlevels - h0;
+    for (int i = 0; i < A.nlevels; ++i) {
+        const int h = h0 + i;
         const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
         const int mo = p->max_own[h], mf = p->max_f[h];
-        A.lv[h].node0 = node0;
-        A.lv[h].cnt = std::max(cnt, 0);
-        A.lv[h].ns = (mo + SB - 1) / SB;
+        A.lv[i].node0 = node0;
+        A.lv[i].cnt = std::max(cnt, 0);
+        A.lv[i].ns = (mo + SB - 1) / SB;
         // boundary rows of a front are at most f - n <= max_f of the height
-        A.lv[h].nbs = (mf + SB - 1) / SB;
+        A.lv[i].nbs = (mf + SB - 1) / SB;
     }
     const size_t smem = sweep_smem(sizeof(T));
     if ((e = ensure_smem((const void *)sweep_kernel<T>, smem))) return e;
@@ -256,6 +262,7 @@ static int solve_sweep(const tf_nd_plan *p, const T *fronts, const int32_t *piv,
     if (cudaMemsetAsync(w + 4, 0, work_bytes - 4, s) != cudaSuccess) return TF_ERR_CUDA;
     launched();
     const DevPlan D = dev_plan(p, p->d_rank);
+    if (h0 > 0 && (e = inv_levels<T>(p, D, fronts, piv, x, ybuf, h0, true, s))) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nsm * occ);
     cfg.blockDim = dim3(SW_THREADS);
@@ -269,6 +276,7 @@ static int solve_sweep(const tf_nd_plan *p, const T *fronts, const int32_t *piv,
     if (cudaLaunchKernelEx(&cfg, sweep_kernel<T>, D, fronts, piv, x, ybuf, words, A) != cudaSuccess)
         return TF_ERR_CUDA;
     launched();
+    if (h0 > 0 && (e = inv_levels<T>(p, D, fronts, piv, x, ybuf, h0, false, s))) return e;
     return cuda_status();
 }
 
@@ -287,13 +295,17 @@ extern "C" size_t tf_nd_sweep_workspace_bytes(const tf_nd_plan *plan) {
 }
 
 extern "C" int tf_nd_solve_sweep_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_t *d_piv,
-                                     double *d_x, void *d_work, size_t work_bytes, tf_stream_t stream) {
-    return nd::solve_sweep<double>(plan, d_fronts, d_piv, d_x, d_work, work_bytes, (cudaStream_t)stream);
+                                     double *d_x, void *d_work, size_t work_bytes, int top_heights,
+                                     tf_stream_t stream) {
+    return nd::solve_sweep<double>(plan, d_fronts, d_piv, d_x, d_work, work_bytes, top_heights,
+                                   (cudaStream_t)stream);
 }
 
 extern "C" int tf_nd_solve_sweep_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,
-                                     double *d_x, void *d_work, size_t work_bytes, tf_stream_t stream) {
-    return nd::solve_sweep<float>(plan, d_fronts, d_piv, d_x, d_work, work_bytes, (cudaStream_t)stream);
+                                     double *d_x, void *d_work, size_t work_bytes, int top_heights,
+                                     tf_stream_t stream) {
+    return nd::solve_sweep<float>(plan, d_fronts, d_piv, d_x, d_work, work_bytes, top_heights,
+                                  (cudaStream_t)stream);
 }
 
 extern "C" int tf_nd_sweep_status(void *d_work) {

@@ -36,6 +36,8 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       keep one launch per tree height)
   'Sweep Apply'       with 'Inverse Apply': both sweeps in one cooperative
                       launch, the tree heights separated by grid-wide barriers
+                      (True), or only the k heights nearest the root (an int
+                      k), the others keeping their per-height launches
                       (default False)
   'Dataflow Fuse Tiles', 'Dataflow Chunk Tiles'
                       fronts with at most this many 32x32 factor tiles per

@@ -251,8 +251,8 @@ class _Engine:
 
                 def solve():
                     _lib.check(sweep_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(),
-                                        self.sweep.data_ptr(), self.sweep.numel() * 8, _stream()),
-                               'tf_nd_solve_sweep')
+                                        self.sweep.data_ptr(), self.sweep.numel() * 8, solver.sweep_heights,
+                                        _stream()), 'tf_nd_solve_sweep')
             elif self.flow is not None:
                 flow_fn = lib.tf_nd_solve_flow_f64 if f64 else lib.tf_nd_solve_flow_f32
 
@@ -324,8 +324,11 @@ class Solver:
         self.inverse = inverse
         # dataflow application (one launch for both sweeps) of the inverted factors
         self.flow = flow and inverse
-        # cooperative one-launch application, heights separated by grid barriers
-        self.sweep = sweep and inverse
+        # cooperative one-launch application, heights separated by grid
+        # barriers: True for every height, an int k for the k heights nearest
+        # the root (the others keep their per-height launches)
+        self.sweep = bool(sweep) and inverse
+        self.sweep_heights = 0 if sweep is True else int(sweep or 0)
         self.flow_fuse_tiles = flow_fuse_tiles
         self.flow_chunk_tiles = flow_chunk_tiles
         self.graphs = graphs
