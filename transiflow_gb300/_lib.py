@@ -9,6 +9,7 @@ import ctypes
 import os
 import shutil
 import subprocess
+import threading
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -173,19 +174,24 @@ def load():
     return lib
 
 
+_streams = []
+_streams_lock = threading.Lock()
+
+
 def new_stream(device=None):
-    """A torch stream over a CUDA stream of its own (tf_stream_create),
-    destroyed when the returned object is garbage collected.  Pooled torch
-    streams repeat after a few dozen allocations, and two threads capturing
-    and launching on one CUDA stream break each other's graph capture."""
+    """A torch stream over a CUDA stream of its own (tf_stream_create).
+    Pooled torch streams repeat after a few dozen allocations, and two
+    threads capturing and launching on one CUDA stream break each other's
+    graph capture.  The streams live until the process exits: PyTorch's
+    allocators keep stream handles with the memory used on them, so a
+    destroyed (and later recycled) handle could be touched again."""
     import torch
-    import weakref
     lib = load()
     handle = ctypes.c_void_p()
     check(lib.tf_stream_create(ctypes.byref(handle)), 'tf_stream_create')
-    stream = torch.cuda.ExternalStream(handle.value, device=device)
-    weakref.finalize(stream, lib.tf_stream_destroy, handle)
-    return stream
+    with _streams_lock:
+        _streams.append(handle)
+    return torch.cuda.ExternalStream(handle.value, device=device)
 
 
 def exported_symbols():

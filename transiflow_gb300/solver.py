@@ -554,36 +554,44 @@ class Solver:
             if relres <= self.tol:
                 break
             self._axpby(1.0 / beta, r, 0.0, None, V[0])
-            g = np.zeros(m + 1)
+            # the Hessenberg columns and Givens rotations are a few dozen
+            # scalars per step: plain Python floats (no NumPy call overhead)
+            g = [0.0] * (m + 1)
             g[0] = beta
-            H = np.zeros((m + 1, m))
-            cs = np.zeros(m)
-            sn = np.zeros(m)
+            cols = []
+            cs = [0.0] * m
+            sn = [0.0] * m
             k = 0
             for j in range(m):
                 self._arnoldi_step(op, fac, j)
                 # the CGS2 coefficients and the new vector's norm, one sync
-                hb = self._hbuf[:2 * (j + 1) + 1].cpu().numpy()
-                hh = hb[:j + 1] + hb[j + 1:2 * (j + 1)]
-                hn = math.sqrt(max(float(hb[-1]), 0.0))
-                H[:j + 1, j] = hh
-                H[j + 1, j] = hn
+                hb = self._hbuf[:2 * (j + 1) + 1].tolist()
+                col = [hb[i] + hb[j + 1 + i] for i in range(j + 1)]
+                hn = math.sqrt(max(hb[-1], 0.0))
+                col.append(hn)
                 for i in range(j):
-                    t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
-                    H[i + 1, j] = -sn[i] * H[i, j] + cs[i] * H[i + 1, j]
-                    H[i, j] = t
-                d = math.hypot(H[j, j], H[j + 1, j])
-                cs[j] = H[j, j] / d if d else 1.0
-                sn[j] = H[j + 1, j] / d if d else 0.0
-                H[j, j] = d
-                H[j + 1, j] = 0.0
+                    t = cs[i] * col[i] + sn[i] * col[i + 1]
+                    col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1]
+                    col[i] = t
+                d = math.hypot(col[j], col[j + 1])
+                cs[j] = col[j] / d if d else 1.0
+                sn[j] = col[j + 1] / d if d else 0.0
+                col[j] = d
+                col[j + 1] = 0.0
+                cols.append(col)
                 g[j + 1] = -sn[j] * g[j]
                 g[j] = cs[j] * g[j]
                 its += 1
                 k = j + 1
                 if abs(g[j + 1]) <= self.tol * bn or its >= maxit or hn == 0:
                     break
-            y = np.linalg.solve(np.triu(H[:k, :k]), g[:k]) if k else np.zeros(0)
+            if k:
+                R = np.zeros((k, k))
+                for jj in range(k):
+                    R[:jj + 1, jj] = cols[jj][:jj + 1]
+                y = np.linalg.solve(R, np.asarray(g[:k]))
+            else:
+                y = np.zeros(0)
             yd = torch.as_tensor(-y, dtype=torch.float64).to(b.device)
             # x += Z[:k]^T y
             self._mgs(Z, k, yd, x) if k else None
