@@ -67,6 +67,8 @@ def parse():
     ap.add_argument('--flow-fuse', type=int, default=48, help='dataflow apply: most factor tiles of a warp-task front')
     ap.add_argument('--flow-chunk', type=int, default=24, help='dataflow apply: target tiles per CTA task')
     ap.add_argument('--leaf-cells', type=int, default=48, help='grid cells at which nested dissection stops')
+    ap.add_argument('--reuse-its', type=int, default=None, help="'Reuse Iterations' (default: the backend's)")
+    ap.add_argument('--reuse-drift', type=float, default=None, help="'Reuse Drift' (default: the backend's)")
     ap.add_argument('--sweep-heights', type=int, default=0,
                     help='with --apply sweep: tree heights nearest the root in the cooperative launch (0: all)')
     return ap.parse_args()
@@ -158,7 +160,12 @@ def gpu_arm(args, rank, world, local):
     from transiflow_gb300 import Continuation, Interface, _lib, dist
     torch.cuda.set_device(local)
     lib = _lib.load()
-    params = {'CUDA': {'Factor Precision': args.precision, 'Tolerance': args.tol,
+    tuning = {}
+    if args.reuse_its is not None:
+        tuning['Reuse Iterations'] = args.reuse_its
+    if args.reuse_drift is not None:
+        tuning['Reuse Drift'] = args.reuse_drift
+    params = {'CUDA': {**tuning, 'Factor Precision': args.precision, 'Tolerance': args.tol,
                        'Dataflow Apply': args.apply == 'flow', 'Sweep Apply': (args.sweep_heights or True) if args.apply == 'sweep' else False,
                        'Dataflow Fuse Tiles': args.flow_fuse,
                        'Dataflow Chunk Tiles': args.flow_chunk, 'Leaf Cells': args.leaf_cells}}
