@@ -68,6 +68,7 @@ def parse():
     ap.add_argument('--flow-chunk', type=int, default=24, help='dataflow apply: target tiles per CTA task')
     ap.add_argument('--leaf-cells', type=int, default=48, help='grid cells at which nested dissection stops')
     ap.add_argument('--reuse-its', type=int, default=None, help="'Reuse Iterations' (default: the backend's)")
+    ap.add_argument('--no-inverse', action='store_true', help="'Inverse Apply': False (substitution solves)")
     ap.add_argument('--reuse-drift', type=float, default=None, help="'Reuse Drift' (default: the backend's)")
     ap.add_argument('--sweep-heights', type=int, default=0,
                     help='with --apply sweep: tree heights nearest the root in the cooperative launch (0: all)')
@@ -165,6 +166,8 @@ def gpu_arm(args, rank, world, local):
         tuning['Reuse Iterations'] = args.reuse_its
     if args.reuse_drift is not None:
         tuning['Reuse Drift'] = args.reuse_drift
+    if args.no_inverse:
+        tuning['Inverse Apply'] = False
     params = {'CUDA': {**tuning, 'Factor Precision': args.precision, 'Tolerance': args.tol,
                        'Dataflow Apply': args.apply == 'flow', 'Sweep Apply': (args.sweep_heights or True) if args.apply == 'sweep' else False,
                        'Dataflow Fuse Tiles': args.flow_fuse,

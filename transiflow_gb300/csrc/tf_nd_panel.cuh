@@ -488,10 +488,8 @@ static int launch_panel(const DevPlan &D, int node0, int cnt, int k, int rows, T
 
 // Cluster size for cnt fronts with up to `rows` panel rows: about one CTA per
 // SM in total and at least 32 rows per CTA.
-static int panel_cluster_size(int cnt, int rows, int nsm) {
-    // up to 4 CTAs: measured faster than 8 at 256^2 (fewer messages per column,
-    // the extra rows per CTA cost less than the exchange)
-    int cl = 4;
+static int panel_cluster_size(int cnt, int rows, int nsm, int clmax) {
+    int cl = clmax;
     while (cl > 1 && (cnt * cl > nsm || rows < 32 * cl)) cl >>= 1;
     return cl;
 }
@@ -527,7 +525,9 @@ int panel(const DevPlan &D, int node0, int cnt, int k, int rows, int nsm, T *fro
                  int32_t *info, cudaStream_t s) {
     // one register-held row per thread while a cluster of up to 8 CTAs
     // offers at most 512 rows per CTA
-    for (int cl = panel_cluster_size(cnt, rows, nsm); cl <= 8; cl *= 2) {
+    // register panels: up to 4 CTAs, measured faster than 8 at 256^2 (fewer
+    // messages per column; the extra rows per CTA cost less than the exchange)
+    for (int cl = panel_cluster_size(cnt, rows, nsm, 4); cl <= 8; cl *= 2) {
         int e = TF_ERR_SIZE;
         switch (cl) {
         case 1: e = launch_panel_reg_pt<T, 1>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
@@ -537,8 +537,8 @@ int panel(const DevPlan &D, int node0, int cnt, int k, int rows, int nsm, T *fro
         }
         if (e != TF_ERR_SIZE) return e;
     }
-    // larger panels: rows staged in shared memory
-    for (int cl = panel_cluster_size(cnt, rows, nsm); cl <= 8; cl *= 2) {
+    // larger panels: rows staged in shared memory, spread over up to 8 CTAs
+    for (int cl = panel_cluster_size(cnt, rows, nsm, 8); cl <= 8; cl *= 2) {
         int e = TF_ERR_SIZE;
         switch (cl) {
         case 1: e = launch_panel<T, 1>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
