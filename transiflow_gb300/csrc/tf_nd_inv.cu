@@ -296,6 +296,7 @@ template <typename T, bool FWD>
 __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0, const T *fronts,
                                                             const int32_t *piv, double *x, double *packed) {
     extern __shared__ double s_gather[];   // forward: s[0 .. rmax)
+    pdl_trigger();
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
     const int rfirst = blockIdx.x * VW;
@@ -303,6 +304,17 @@ __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0
     const int32_t *g = P.idx + P.idx_off[node];
     double *pk = packed + P.idx_off[node];
     const double *sv = pk;
+    {
+        // the factors do not change during an application: start their
+        // reads before waiting for the previous launch
+        const int r = rfirst + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+        if (r < n) {
+            const T *row = fronts + P.front_off[node] + (size_t)r * f;
+            const int c0 = FWD ? 0 : r, c1 = FWD ? r : n;
+            for (int c = c0 + lane * (128 / sizeof(T)); c < c1; c += 32 * (128 / sizeof(T))) prefetch_l2(row + c);
+        }
+    }
+    pdl_wait();
     if (FWD) {
         const int rmax = min(n, rfirst + VW);
         const int32_t *pv = piv + P.piv_off[node];
@@ -343,11 +355,19 @@ template <typename T, bool FWD>
 __global__ void __launch_bounds__(VT) inv_apply_rows_kernel(DevPlan P, int node0, const T *fronts,
                                                             const int32_t *piv, double *x, double *packed) {
     __shared__ double s_gather[VS];
+    pdl_trigger();
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
     const int32_t *g = P.idx + P.idx_off[node];
     double *pk = packed + P.idx_off[node];
     const double *sv = pk;
+    if (threadIdx.x < n) {
+        // this thread's row of the factors, before the wait
+        const T *row = fronts + P.front_off[node] + (size_t)threadIdx.x * f;
+        const int c0 = FWD ? 0 : threadIdx.x, c1 = FWD ? threadIdx.x : n;
+        for (int c = c0; c < c1; c += 128 / sizeof(T)) prefetch_l2(row + c);
+    }
+    pdl_wait();
     if (FWD) {
         const int32_t *pv = piv + P.piv_off[node];
         for (int c = threadIdx.x; c < n; c += VT) s_gather[c] = x[g[pv[c]]];
@@ -387,6 +407,7 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node
     extern __shared__ unsigned char smem_raw[];
     T *tiles = reinterpret_cast<T *>(smem_raw);   // [BV_WARPS][2] tiles
     __shared__ T v[BV_TILES * SB];
+    pdl_trigger();
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
     const int rlo = FWD ? n : 0, rhi = FWD ? f : n;
@@ -402,7 +423,9 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int r0 = rbase + warp * SB;
     T *b0 = tiles + (2 * warp) * TILE, *b1 = b0 + TILE;
+    // the first tile of the factors, before waiting for the previous launch
     if (r0 < rhi) tile_issue(b0, F, f, r0, rhi, cbase, chi, lane);
+    pdl_wait();
     for (int c = threadIdx.x; c < ccols; c += BV_THREADS)
         v[c] = cbase + c < cend ? (T)(FWD ? pk[cbase + c] : x[g[cbase + c]]) : T(0);
     __syncthreads();
@@ -427,36 +450,42 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node
     }
 }
 
+// The products of one application are launched with programmatic stream
+// serialisation (pdl: every launch but the first of the sequence), so each
+// starts reading its factors while the one before it finishes.
 template <typename T, bool FWD>
 static int inv_apply(const DevPlan &D, int node0, int cnt, int mo, const T *fronts, const int32_t *piv, double *x,
-                     double *packed, cudaStream_t s) {
+                     double *packed, bool pdl, cudaStream_t s) {
+    cudaError_t ce;
     // FP32 shuffles are cheap, so single precision always takes a warp per row
     if (sizeof(T) == 8 && mo <= VS && cnt >= 256) {
-        inv_apply_rows_kernel<T, FWD><<<dim3(1, cnt), VT, 0, s>>>(D, node0, fronts, piv, x, packed);
+        ce = launch_pdl(pdl, inv_apply_rows_kernel<T, FWD>, dim3(1, cnt), dim3(VT), 0, s, D, node0, fronts, piv, x,
+                        packed);
     } else {
         const size_t sm = FWD ? sizeof(double) * (size_t)mo : 0;
         if (sm > 48 * 1024) {
             const int e = ensure_smem((const void *)inv_apply_kernel<T, FWD>, sm);
             if (e) return e;
         }
-        inv_apply_kernel<T, FWD><<<dim3((mo + VW - 1) / VW, cnt), 32 * VW, sm, s>>>(D, node0, fronts, piv, x,
-                                                                                   packed);
+        ce = launch_pdl(pdl, inv_apply_kernel<T, FWD>, dim3((mo + VW - 1) / VW, cnt), dim3(32 * VW), sm, s, D, node0,
+                        fronts, piv, x, packed);
     }
     launched();
-    return TF_OK;
+    return ce == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
 
 template <typename T, bool FWD>
-static void inv_bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, int nsm, const T *fronts, double *x,
-                    double *packed, cudaStream_t s) {
-    if (rows <= 0 || cols <= 0) return;
+static int inv_bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, int nsm, const T *fronts, double *x,
+                   double *packed, bool pdl, cudaStream_t s) {
+    if (rows <= 0 || cols <= 0) return TF_OK;
     const int rb = (rows + BV_ROWS - 1) / BV_ROWS;
     const int wide = rb * cnt * ((cols + BV_TILES * SB - 1) / (BV_TILES * SB));
     const int ctiles = wide >= 4 * nsm ? BV_TILES : 1;
     dim3 grid(rb, cnt, (cols + ctiles * SB - 1) / (ctiles * SB));
-    inv_bnd_kernel<T, FWD><<<grid, BV_THREADS, sizeof(T) * 2 * BV_WARPS * TILE, s>>>(D, node0, ctiles, fronts, x,
-                                                                                     packed);
+    const cudaError_t ce = launch_pdl(pdl, inv_bnd_kernel<T, FWD>, grid, dim3(BV_THREADS),
+                                      sizeof(T) * 2 * BV_WARPS * TILE, s, D, node0, ctiles, fronts, x, packed);
     launched();
+    return ce == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
 
 template <typename T>
@@ -467,18 +496,20 @@ int inv_levels(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return TF_ERR_CUDA;
     h_end = std::min(h_end, p->nlevels);
+    bool first = true;   // the sequence's first launch waits for everything before it
     for (int i = 0; i < h_end; ++i) {
         const int h = fwd ? i : h_end - 1 - i;
         const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
         const int mo = p->max_own[h], mf = p->max_f[h];
         if (cnt <= 0 || mo <= 0) continue;
         if (fwd) {
-            if ((e = inv_apply<T, true>(D, node0, cnt, mo, fronts, piv, x, packed, s))) return e;
-            inv_bnd<T, true>(D, node0, cnt, mf, mo, nsm, fronts, x, packed, s);
+            if ((e = inv_apply<T, true>(D, node0, cnt, mo, fronts, piv, x, packed, !first, s))) return e;
+            if ((e = inv_bnd<T, true>(D, node0, cnt, mf, mo, nsm, fronts, x, packed, true, s))) return e;
         } else {
-            inv_bnd<T, false>(D, node0, cnt, mo, mf, nsm, fronts, x, packed, s);
-            if ((e = inv_apply<T, false>(D, node0, cnt, mo, fronts, piv, x, packed, s))) return e;
+            if ((e = inv_bnd<T, false>(D, node0, cnt, mo, mf, nsm, fronts, x, packed, !first, s))) return e;
+            if ((e = inv_apply<T, false>(D, node0, cnt, mo, fronts, piv, x, packed, true, s))) return e;
         }
+        first = false;
     }
     return cuda_status();
 }
