@@ -295,7 +295,7 @@ constexpr int VW = 8;              // rows (one warp each) per CTA of the warp k
 template <typename T, bool FWD>
 __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0, const T *fronts,
                                                             const int32_t *piv, double *x, double *packed) {
-    extern __shared__ double s_gather[];   // forward: s[0 .. rmax)
+    extern __shared__ double s_gather[];   // forward: s[0 .. rmax), then their indices in x
     pdl_trigger();
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
@@ -314,11 +314,16 @@ __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0
             for (int c = c0 + lane * (128 / sizeof(T)); c < c1; c += 32 * (128 / sizeof(T))) prefetch_l2(row + c);
         }
     }
+    // the positions in x of s (pivot order) do not depend on earlier launches
+    const int rmax = min(n, rfirst + VW);
+    int32_t *s_idx = reinterpret_cast<int32_t *>(s_gather + rmax);
+    if (FWD) {
+        const int32_t *pv = piv + P.piv_off[node];
+        for (int c = threadIdx.x; c < rmax; c += 32 * VW) s_idx[c] = g[pv[c]];
+    }
     pdl_wait();
     if (FWD) {
-        const int rmax = min(n, rfirst + VW);
-        const int32_t *pv = piv + P.piv_off[node];
-        for (int c = threadIdx.x; c < rmax; c += 32 * VW) s_gather[c] = x[g[pv[c]]];
+        for (int c = threadIdx.x; c < rmax; c += 32 * VW) s_gather[c] = x[s_idx[c]];
         __syncthreads();
         sv = s_gather;
     }
@@ -367,10 +372,11 @@ __global__ void __launch_bounds__(VT) inv_apply_rows_kernel(DevPlan P, int node0
         const int c0 = FWD ? 0 : threadIdx.x, c1 = FWD ? threadIdx.x : n;
         for (int c = c0; c < c1; c += 128 / sizeof(T)) prefetch_l2(row + c);
     }
+    // the position in x of this thread's entry of s (pivot order) before the wait
+    const int32_t xi = (FWD && threadIdx.x < n) ? g[piv[P.piv_off[node] + threadIdx.x]] : 0;
     pdl_wait();
     if (FWD) {
-        const int32_t *pv = piv + P.piv_off[node];
-        for (int c = threadIdx.x; c < n; c += VT) s_gather[c] = x[g[pv[c]]];
+        if (threadIdx.x < n) s_gather[threadIdx.x] = x[xi];
         __syncthreads();
         sv = s_gather;
     }
@@ -423,11 +429,22 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int r0 = rbase + warp * SB;
     T *b0 = tiles + (2 * warp) * TILE, *b1 = b0 + TILE;
-    // the first tile of the factors, before waiting for the previous launch
+    // the first tile of the factors and the vector's positions, before
+    // waiting for the previous launch
     if (r0 < rhi) tile_issue(b0, F, f, r0, rhi, cbase, chi, lane);
+    constexpr int PER = BV_TILES * SB / BV_THREADS;
+    int32_t vi[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int c = threadIdx.x + q * BV_THREADS;
+        vi[q] = (c < ccols && cbase + c < cend) ? (FWD ? cbase + c : g[cbase + c]) : -1;
+    }
     pdl_wait();
-    for (int c = threadIdx.x; c < ccols; c += BV_THREADS)
-        v[c] = cbase + c < cend ? (T)(FWD ? pk[cbase + c] : x[g[cbase + c]]) : T(0);
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int c = threadIdx.x + q * BV_THREADS;
+        if (c < ccols) v[c] = vi[q] >= 0 ? (T)(FWD ? pk[vi[q]] : x[vi[q]]) : T(0);
+    }
     __syncthreads();
     if (r0 >= rhi) return;
     T s = T(0);
@@ -462,7 +479,7 @@ static int inv_apply(const DevPlan &D, int node0, int cnt, int mo, const T *fron
         ce = launch_pdl(pdl, inv_apply_rows_kernel<T, FWD>, dim3(1, cnt), dim3(VT), 0, s, D, node0, fronts, piv, x,
                         packed);
     } else {
-        const size_t sm = FWD ? sizeof(double) * (size_t)mo : 0;
+        const size_t sm = FWD ? (sizeof(double) + sizeof(int32_t)) * (size_t)mo : 0;
         if (sm > 48 * 1024) {
             const int e = ensure_smem((const void *)inv_apply_kernel<T, FWD>, sm);
             if (e) return e;
