@@ -222,6 +222,9 @@ int tf_vec_axpby(int n, double a, const double *d_x, double b, const double *d_y
                  double *d_z, tf_stream_t stream);
 /* z = x / s, IEEE division per element (z may alias x).                      */
 int tf_vec_div(int n, const double *d_x, double s, double *d_z, tf_stream_t stream);
+/* d_z *= 1 / sqrt(*d_nrm2) with the square norm read on the device (the
+ * normalisation of an Arnoldi vector without a host round trip).            */
+int tf_vec_scale_rsqrt(int n, const double *d_nrm2, double *d_z, tf_stream_t stream);
 int tf_vec_fill(int n, double a, double *d_z, tf_stream_t stream);
 int tf_vec_to_f32(int n, const double *d_x, float *d_y, tf_stream_t stream);
 

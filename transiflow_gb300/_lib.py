@@ -125,6 +125,7 @@ _SIGNATURES = {
     'tf_vec_axpby': ([_I, _D, _P, _D, _P, _P, _P], _I),
     'tf_vec_div': ([_I, _P, _D, _P, _P], _I),
     'tf_vec_fill': ([_I, _D, _P, _P], _I),
+    'tf_vec_scale_rsqrt': ([_I, _P, _P, _P], _I),
     'tf_vec_to_f32': ([_I, _P, _P, _P], _I),
     'tf_nd_factor_f64': ([_P, _P, _P, _P, _P, _P], _I),
     'tf_nd_factor_f32': ([_P, _P, _P, _P, _P, _P], _I),

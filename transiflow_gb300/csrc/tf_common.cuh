@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <utility>
 
 #include "../../include/tfcuda.h"
 
@@ -21,6 +22,35 @@ static inline void launched(long long k = 1) { g_launches.fetch_add(k, std::memo
 static inline int cuda_status() {
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation may start while the previous kernel of the stream runs;
+// pdl_trigger lets the next launch start, pdl_wait blocks until the previous
+// kernel has finished and its writes are visible (a no-op without the
+// attribute).  Work before pdl_wait may only touch data no earlier launch of
+// the sequence writes.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
+}
+
+// Launch with or without programmatic stream serialisation.
+template <typename... KArgs, typename... Args>
+static inline cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                     cudaStream_t s, Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 __host__ __device__ constexpr int off_index(int ox, int oy, int oz) { return ox + 3 * oy + 9 * oz; }

@@ -243,6 +243,13 @@ __global__ void div_kernel(int n, const double *x, double s, double *z) {
     if (i < n) z[i] = x[i] / s;
 }
 
+// z *= 1 / sqrt(*nrm2), the square norm read on the device (a zero norm
+// makes z non-finite: a breakdown the caller detects).
+__global__ void scale_rsqrt_kernel(int n, const double *nrm2, double *z) {
+    const double r = rsqrt(*nrm2);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) z[i] *= r;
+}
+
 __global__ void fill_kernel(int n, double a, double *z) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) z[i] = a;
@@ -432,7 +439,7 @@ extern "C" int tf_vec_mdot_noalloc(int n, int k, const double *d_V, long long ld
     int nb = blocks_for(n, RED_THREADS);
     if (nb > RED_BLOCKS) nb = RED_BLOCKS;
     mdot_partial_kernel<<<nb, RED_THREADS, 0, s>>>(n, k, d_V, ldv, d_w, scratch); launched();
-    mdot_final_kernel<<<k, 128, 0, s>>>(nb, k, scratch, d_out); launched();
+    mdot_final_kernel<<<k, 128, 0, s>>>(nb, k, (const double *)scratch, d_out); launched();
     return cuda_status();
 }
 
@@ -448,6 +455,13 @@ extern "C" int tf_vec_axpby(int n, double a, const double *d_x, double b, const 
 extern "C" int tf_vec_div(int n, const double *d_x, double s, double *d_z, tf_stream_t stream) {
     if (n <= 0 || !d_x || !d_z) return TF_ERR_ARG;
     div_kernel<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, d_x, s, d_z); launched();
+    return cuda_status();
+}
+
+extern "C" int tf_vec_scale_rsqrt(int n, const double *d_nrm2, double *d_z, tf_stream_t stream) {
+    if (n <= 0 || !d_nrm2 || !d_z) return TF_ERR_ARG;
+    scale_rsqrt_kernel<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, d_nrm2, d_z);
+    launched();
     return cuda_status();
 }
 

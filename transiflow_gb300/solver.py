@@ -521,7 +521,8 @@ class Solver:
                 self._mgs(V, j + 1, h2, w)
                 self._mdot_into(w.view(1, -1), 1, w, ww)
                 # a zero norm (breakdown) makes w non-finite; the caller stops there
-                torch.mul(w, torch.rsqrt(ww), out=w)
+                _lib.check(lib.tf_vec_scale_rsqrt(w.numel(), ww.data_ptr(), w.data_ptr(), _stream()),
+                           'tf_vec_scale_rsqrt')
 
             step = _Graphed(fn, self.stats) if self.graphs else fn
             self._steps[key] = step
