@@ -429,9 +429,12 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int r0 = rbase + warp * SB;
     T *b0 = tiles + (2 * warp) * TILE, *b1 = b0 + TILE;
-    // the first tile of the factors and the vector's positions, before
+    // the first two tiles of the factors and the vector's positions, before
     // waiting for the previous launch
-    if (r0 < rhi) tile_issue(b0, F, f, r0, rhi, cbase, chi, lane);
+    if (r0 < rhi) {
+        tile_issue(b0, F, f, r0, rhi, cbase, chi, lane);
+        if (cbase + SB < cend) tile_issue(b1, F, f, r0, rhi, cbase + SB, chi, lane);
+    }
     constexpr int PER = BV_TILES * SB / BV_THREADS;
     int32_t vi[PER];
 #pragma unroll
@@ -447,19 +450,20 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node
     }
     __syncthreads();
     if (r0 >= rhi) return;
+    // tiles t and t + 1 are in flight while tile t is multiplied; tile t + 2
+    // then goes into tile t's buffer
     T s = T(0);
     int t = 0;
     for (int c0 = cbase; c0 < cend; c0 += SB, ++t) {
         T *cur = (t & 1) ? b1 : b0;
-        if (c0 + SB < cend) {
-            tile_issue((t & 1) ? b0 : b1, F, f, r0, rhi, c0 + SB, chi, lane);
+        if (c0 + SB < cend)
             cp_async_wait<1>();
-        } else {
+        else
             cp_async_wait<0>();
-        }
         __syncwarp();
         s += tile_dot(cur, v + (c0 - cbase), lane);
         __syncwarp();
+        if (c0 + 2 * SB < cend) tile_issue(cur, F, f, r0, rhi, c0 + 2 * SB, chi, lane);
     }
     if (r0 + lane < rhi) {
         if (FWD) atomicAdd(x + g[r0 + lane], -(double)s);
