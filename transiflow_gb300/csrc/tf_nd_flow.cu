@@ -1,10 +1,10 @@
 // Dataflow application of the inverted factors (after tf_nd_invert_*): the
 // forward and the backward sweep of every front in ONE persistent launch.
 //
-// The height-by-height application (tf_nd_solve_inv_*) issues a gather, a
-// product with the inverted own block and a boundary product per height and
-// sweep.  Near the root each of those launches holds a handful of fronts and
-// most SMs wait for the launch boundary.  Here the work is a list of tasks in
+// The height-by-height application (tf_nd_solve_inv_*) issues a product with
+// the inverted own block and a boundary product per height and sweep.  Near
+// the root each of those launches holds a handful of fronts and most SMs wait
+// for the launch boundary.  Here the work is a list of tasks in
 // an order compatible with the elimination tree; CTAs take tasks in list order
 // from an atomic ticket, and a task waits (bounded spin) only for the tasks it
 // depends on, through per-front counters:
@@ -16,11 +16,13 @@
 //                       backward own-row tasks (the root: its forward);
 //            own rows   x[own] = U11^-1 t, waits for the front's boundary tasks.
 //
-// Fronts whose factors fit in few tiles run both parts of a sweep in one task.
-// A task covers up to FSPT 32-row strips; its 8 warps share the (strip, tile)
-// pairs, each warp double-buffering 32 x 32 tiles with cp.async and every lane
-// forming one row's dot product serially (no FP64 shuffles).  Tiles are issued
-// before the dependency wait: the factors do not change during the launch.
+// Fronts whose factors fit in few tiles go to bundle tasks: up to FW fronts
+// of one height, one warp each doing both parts of the sweep.  The other
+// tasks cover up to FSPT 32-row strips of one front; the CTA's 8 warps share
+// the (strip, tile) pairs.  Each warp double-buffers 32 x 32 tiles with
+// cp.async and every lane forms one row's dot product serially (no FP64
+// shuffles).  Tiles are issued before the dependency wait: the factors do not
+// change during the launch.  (Opt-in: the per-height launches measured faster.)
 //
 // Deadlock freedom does not depend on how many CTAs are resident: a task only
 // waits for tasks earlier in the list, which were taken by CTAs already
