@@ -8,8 +8,9 @@
 // triangles are therefore inverted once per factorisation (in place: the
 // inverse of the unit lower part keeps the strictly lower positions, the
 // inverse of the upper part the upper ones), and an application becomes a
-// gather plus a triangular matrix-vector product per tree height, parallel
-// over all rows.
+// triangular matrix-vector product (with the gather of its right-hand side
+// folded in) and a boundary product per tree height and sweep, parallel over
+// all rows.
 //
 // Inversion by recursive halving of each own block: a segment of m rows
 // (m > 32) splits at m1 = 32 ceil(nb / 2) (nb = ceil(m / 32) row blocks),
