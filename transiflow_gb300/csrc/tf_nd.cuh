@@ -72,6 +72,16 @@ __device__ __forceinline__ T tile_dot(const T *buf, const T *v, int lane) {
     return s;
 }
 
+// The same over the first nc <= SB columns only (a front's last, partial
+// column tile: the FP64 pipe then does only the useful products).
+template <typename T>
+__device__ __forceinline__ T tile_dot_n(const T *buf, const T *v, int lane, int nc) {
+    if (nc >= SB) return tile_dot(buf, v, lane);
+    T s = T(0);
+    for (int c = 0; c < nc; ++c) s += buf[lane * TSTRIDE + c] * v[c];
+    return s;
+}
+
 // Opts a kernel in to `bytes` of dynamic shared memory on the current device
 // (TF_ERR_SIZE when static plus dynamic shared memory would not fit).
 int ensure_smem(const void *kernel, size_t bytes);

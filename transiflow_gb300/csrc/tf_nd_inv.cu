@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node
         else
             cp_async_wait<0>();
         __syncwarp();
-        s += tile_dot(cur, v + (c0 - cbase), lane);
+        s += tile_dot_n(cur, v + (c0 - cbase), lane, cend - c0);
         __syncwarp();
         if (c0 + 2 * SB < cend) tile_issue(cur, F, f, r0, rhi, c0 + 2 * SB, chi, lane);
     }
