@@ -69,3 +69,18 @@ def test_time_integration_returns_to_steady_state():
         x3, t = ti.integration(x2, 100, 1000)
     assert np.linalg.norm(xs[0::3] - x3.numpy()[0::3]) < 1e-4
     assert np.linalg.norm(xs[1::3] - x3.numpy()[1::3]) < 1e-4
+
+
+def test_save_and_load_state_round_trip(tmp_path):
+    """save_state / load_state (the reference's checkpoint format: a .npy state
+    and a .params JSON file) restore the state and the parameters."""
+    import numpy as np
+    from transiflow_gb300 import Interface
+    itf = Interface({'Reynolds Number': 250}, 8, 6)
+    x = itf.vector_from_array(np.random.default_rng(9).standard_normal(itf.n))
+    name = str(tmp_path / 'point')
+    itf.save_state(name, x)
+    other = Interface({'Reynolds Number': 10}, 8, 6)
+    y = other.load_state(name)
+    assert other.get_parameter('Reynolds Number') == 250
+    assert np.array_equal(other.array_from_vector(y), itf.array_from_vector(x))

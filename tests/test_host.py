@@ -285,3 +285,20 @@ def test_dataflow_task_list_follows_the_elimination_tree(built_lib, case, fuse, 
         else:
             need = mask([i], (K_BBND,))
         assert need & ~done[k] == 0
+
+
+def test_parameter_files_round_trip(tmp_path):
+    """Parameters saved with a state (the reference's save_parameters /
+    load_parameters format, BaseInterface.py:84-160) survive NumPy scalars,
+    arrays and complex values."""
+    from transiflow_gb300.interface import Interface
+    params = {'Reynolds Number': np.float64(1500.0), 'Problem Type': 'Lid-driven Cavity',
+              'Grid Stretching Factor': 1.5, 'Count': np.int32(3), 'Shift': 1 + 2j,
+              'Profile': np.arange(3.0)}
+    name = str(tmp_path / 'state')
+    Interface.save_json(None, name + '.params', params)
+    back = Interface.load_json(None, name + '.params')
+    assert back['Reynolds Number'] == 1500.0 and back['Count'] == 3
+    assert back['Shift'] == 1 + 2j
+    assert back['Profile'] == [0.0, 1.0, 2.0]
+    assert back['Problem Type'] == 'Lid-driven Cavity' and back['Grid Stretching Factor'] == 1.5
