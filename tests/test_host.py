@@ -110,6 +110,27 @@ def test_c_abi_exports_every_declared_symbol(built_lib):
         assert ctypes.cast(getattr(built_lib, name), ctypes.c_void_p).value
 
 
+def test_python_binding_matches_the_header():
+    """Every entry point the ctypes binding declares is in the header with
+    the same number of parameters and a matching return type (the binding
+    cannot drift from the C ABI a foreign caller sees)."""
+    from transiflow_gb300 import _lib
+    hdr = open(os.path.join(ROOT, 'include', 'tfcuda.h')).read()
+    hdr = re.sub(r'/\*.*?\*/', '', hdr, flags=re.S)
+    protos = {}
+    for m in re.finditer(r'^\s*(int|size_t|long long|void|const char \*)\s*(tf_\w+)\s*\(([^;]*?)\)\s*;', hdr, re.M | re.S):
+        ret, name, args = m.group(1), m.group(2), ' '.join(m.group(3).split())
+        n = 0 if args in ('', 'void') else args.count(',') + 1
+        protos[name] = (ret, n)
+    rets = {'int': ctypes.c_int, 'size_t': ctypes.c_size_t, 'long long': ctypes.c_longlong, 'void': None,
+            'const char *': ctypes.c_char_p}
+    for name, (args, res) in _lib._SIGNATURES.items():
+        assert name in protos, name
+        ret, n = protos[name]
+        assert n == len(args), (name, n, len(args))
+        assert rets[ret] is res, (name, ret, res)
+
+
 def test_boundary_program_records_custom_callback():
     """The reference's test_custom_bc callback (tests/test_interface.py:118-148)."""
     def boundaries(bc, atom):
