@@ -357,6 +357,57 @@ int tf_nd_solve_sweep_f32(const tf_nd_plan *plan, const float *d_fronts, const i
                           tf_stream_t stream);
 int tf_nd_sweep_status(void *d_work);
 
+/* ---- learned continuation predictor ---------------------------------------
+ * A stack of 3x3x3 convolutions over the cell grid proposing the correction
+ * to the secant predictor (x0 + ds*t) of pseudo-arclength continuation; the
+ * reference has only the secant predictor (transiflow/Continuation.py:
+ * 258-260), so these entry points replace none of its interfaces.
+ * Activations are channels-last BF16 [cell][kp], cell = i + nx*(j + ny*k);
+ * kp and np (channels in and out) are 16 or 32.  Weights: forward layout
+ * BF16 [27][np][kp]; backward-data layout BF16 [27][kp][np] holding the
+ * mirrored tap (26 - tap); FP32 master weights [27][kp][np] and bias [np];
+ * gradients and Adam moments FP32 [28][kp][np] (slot 27, row 0: the bias).
+ *
+ * tf_sg_conv: Z = conv(X, W) + bias (FP32 [cell][np], nullable) and A =
+ *   relu(Z) if relu else Z (BF16 [cell][np], nullable; not both null);
+ *   d_bias may be null (no bias).  With the backward-data weights and dZ as
+ *   X it computes the gradient with respect to the layer's input.
+ * tf_sg_wgrad: grad (+)= d loss / d (w, bias) from the layer input X (BF16
+ *   [cell][kp]) and dZ (FP32 [cell][np]); a per-chunk partial sum in d_work
+ *   (tf_sg_wgrad_workspace_bytes), reduced in a fixed order.
+ * tf_sg_loss: loss[0] = mean over cells and the first dof channels of
+ *   (out - tgt)^2, with dZ = d loss / d out in FP32 and BF16; d_work:
+ *   tf_sg_loss_workspace_bytes.
+ * tf_sg_act_grad: dZ = dA where Z > 0 else 0, FP32 and BF16 (n elements).
+ * tf_sg_pack: the network input from the FP64 state x and tangent t (scaled
+ *   by the host arrays sx, st of dof entries), the parameter mu and step ds.
+ * tf_sg_target: tgt = (x1 - x0 - ds t) * inv_scale[d] (FP32).
+ * tf_sg_unpack: xp = x0 + ds t + scale[d] * out[cell][d] (FP64); entries
+ *   whose tangent t is exactly zero (unknowns the branch does not move, such
+ *   as the pressure gauge) get x0 + ds t only.
+ * tf_sg_adam: one Adam step (step >= 1, bias-corrected) of the master
+ *   weights with the gradient scaled by grad_scale, then both BF16 layouts;
+ *   step 0 only writes the BF16 layouts (d_grad, d_m, d_v may be null).    */
+int tf_sg_conv(int nx, int ny, int nz, int kp, int np, const void *d_x, const void *d_w, const float *d_bias,
+               float *d_z, void *d_a, int relu, tf_stream_t stream);
+size_t tf_sg_wgrad_workspace_bytes(int ncell, int kp, int np);
+int tf_sg_wgrad(int nx, int ny, int nz, int kp, int np, const void *d_x, const float *d_dz, float *d_grad,
+                int accumulate, void *d_work, size_t work_bytes, tf_stream_t stream);
+size_t tf_sg_loss_workspace_bytes(int ncell, int np);
+int tf_sg_loss(int ncell, int dof, int np, const float *d_out, const float *d_tgt, float *d_dzf, void *d_dzh,
+               double *d_loss, void *d_work, size_t work_bytes, tf_stream_t stream);
+int tf_sg_act_grad(long long n, const float *d_da, const float *d_z, float *d_dzf, void *d_dzh,
+                   tf_stream_t stream);
+int tf_sg_pack(int ncell, int dof, int kp, const double *d_x, const double *d_t, const float *sx,
+               const float *st, float mu, float ds, void *d_x0, tf_stream_t stream);
+int tf_sg_target(int ncell, int dof, const double *d_x0, const double *d_t, const double *d_x1, double ds,
+                 const double *inv_scale, float *d_tgt, tf_stream_t stream);
+int tf_sg_unpack(int ncell, int dof, int np, const float *d_out, const double *d_x0, const double *d_t,
+                 double ds, const double *scale, double *d_xp, tf_stream_t stream);
+int tf_sg_adam(int kp, int np, float *d_w, float *d_bias, const float *d_grad, float *d_m, float *d_v,
+               float lr, float beta1, float beta2, float eps, int step, float grad_scale, void *d_wf,
+               void *d_wb, tf_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,282 @@
+"""The learned continuation predictor: its convolution, gradients and Adam
+step against the CPU oracle (PyTorch conv3d and autograd in FP32), what the
+trained network gains over the secant predictor on a 2D lid-driven cavity
+branch, and the continuation's fallback to the secant predictor."""
+
+import ctypes
+import time
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import surrogate as ref
+
+
+# -- CPU: the oracle's conventions and the continuation's fallback ----------------
+
+@pytest.mark.parametrize('dims', [(4, 3, 2), (5, 4, 1), (3, 3, 3)])
+def test_oracle_convolution_matches_explicit_loops(dims):
+    """The torch conv3d route of the oracle agrees with explicit loops over
+    cells and taps (cell = i + nx*(j + ny*k), tap = (ox+1) + 3(oy+1) + 9(oz+1))."""
+    g = torch.Generator().manual_seed(0)
+    ncell = dims[0] * dims[1] * dims[2]
+    x = torch.randn(ncell, 16, generator=g, dtype=torch.float64)
+    w = torch.randn(27, 16, 8, generator=g, dtype=torch.float64)
+    b = torch.randn(8, generator=g, dtype=torch.float64)
+    z = ref.conv(x, w, b, dims).numpy()
+    assert np.allclose(z, ref.conv_loops(x.numpy(), w.numpy(), b.numpy(), dims), rtol=1e-12, atol=1e-12)
+
+
+class _Cubic:
+    """A two-unknown problem F(x, mu) = (x0^3 + x0 - mu, x1 - mu/2) with the
+    interface calls the continuation makes, on NumPy vectors."""
+
+    def __init__(self):
+        self.mu = 0.0
+
+    def set_parameter(self, name, value):
+        self.mu = value
+
+    def get_parameter(self, name):
+        return self.mu
+
+    def rhs(self, x):
+        return np.array([x[0] ** 3 + x[0] - self.mu, x[1] - 0.5 * self.mu])
+
+    def jacobian(self, x):
+        return np.array([[3 * x[0] ** 2 + 1, 0.0], [0.0, 1.0]])
+
+    def solve(self, jac, rhs, *args):
+        return np.linalg.solve(jac, rhs)
+
+
+@pytest.mark.parametrize('quality', ['exact', 'wrong'])
+def test_continuation_falls_back_to_the_secant_predictor(quality):
+    """A predictor the corrector accepts is counted as accepted; one whose
+    corrector does not converge within the learned iteration limit is
+    rejected and the step is redone from the secant predictor, reaching the
+    same branch end."""
+    from transiflow_gb300.continuation import Continuation
+
+    def exact(interface, x0, mu0, dx, dmu, ds):
+        mu = mu0 + ds * dmu
+        r = np.roots([1, 0, 1, -mu]).real.max()
+        return np.array([r, 0.5 * mu]), mu
+
+    def wrong(interface, x0, mu0, dx, dmu, ds):
+        return np.array([1e6, -1e6]), mu0 + ds * dmu
+
+    itf = _Cubic()
+    plain = Continuation(itf, newton_tolerance=1e-10, quiet=True)
+    xp, mup = plain.continuation(np.zeros(2), 'mu', 0.0, 10.0, 0.5)
+    itf = _Cubic()
+    cont = Continuation(itf, newton_tolerance=1e-10, quiet=True,
+                        predictor=exact if quality == 'exact' else wrong)
+    x, mu = cont.continuation(np.zeros(2), 'mu', 0.0, 10.0, 0.5)
+    assert abs(mu - 10.0) < 1e-4 and abs(mup - 10.0) < 1e-4
+    for xx, mm in ((x, mu), (xp, mup)):
+        r = np.roots([1, 0, 1, -mm]).real.max()
+        assert np.allclose(xx, [r, 0.5 * mm], rtol=1e-9, atol=1e-9)
+    if quality == 'exact':
+        assert cont.stats['learned_accepted'] > 0 and cont.stats['learned_rejected'] == 0
+    else:
+        assert cont.stats['learned_accepted'] == 0 and cont.stats['learned_rejected'] > 0
+
+
+# -- GPU: the kernels against the oracle ---------------------------------------
+
+def _lib():
+    from transiflow_gb300 import _lib as L
+    return L, L.load()
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('dims,kp,np_', [((7, 5, 3), 16, 32), ((9, 7, 1), 32, 32), ((6, 6, 2), 32, 16),
+                                          ((5, 3, 4), 16, 16), ((33, 17, 1), 32, 32)])
+def test_convolution_matches_the_oracle(dims, kp, np_):
+    """Forward convolution (BF16 operands, FP32 accumulation) against the
+    oracle on the same BF16 values: sums of exact products, so only the
+    summation order differs (relative 1e-5)."""
+    L, lib = _lib()
+    g = torch.Generator().manual_seed(1)
+    ncell = dims[0] * dims[1] * dims[2]
+    x = ref.bf16(torch.randn(ncell, kp, generator=g))
+    w = ref.bf16(torch.randn(27, kp, np_, generator=g) * 0.2)
+    b = torch.randn(np_, generator=g)
+    dx = x.to(torch.bfloat16).cuda()
+    dwf = w.permute(0, 2, 1).contiguous().to(torch.bfloat16).cuda()
+    db = b.cuda()
+    z = torch.empty(ncell, np_, dtype=torch.float32, device='cuda')
+    a = torch.empty(ncell, np_, dtype=torch.bfloat16, device='cuda')
+    L.check(lib.tf_sg_conv(*dims, kp, np_, dx.data_ptr(), dwf.data_ptr(), db.data_ptr(), z.data_ptr(),
+                           a.data_ptr(), 1, _stream()), 'tf_sg_conv')
+    torch.cuda.synchronize()
+    zr = ref.conv(x.double(), w.double(), b.double(), dims)
+    zg = z.cpu().double()
+    assert (zg - zr).abs().max() <= 1e-5 * zr.abs().max()
+    assert torch.equal(a.cpu(), torch.relu(z.cpu()).to(torch.bfloat16))
+
+
+def _surrogate(dof, seed, layers=4, channels=32):
+    from transiflow_gb300.surrogate import Surrogate
+    s = Surrogate(dof, channels=channels, layers=layers, seed=seed)
+    # a non-zero last layer, so that gradients reach every layer
+    g = torch.Generator().manual_seed(seed + 100)
+    w = torch.zeros_like(s.w[-1], device='cpu')
+    w[:, :, :dof] = (torch.rand(27, s.kp[-1], dof, generator=g) * 2 - 1) * 0.05
+    s.w[-1].copy_(w)
+    s.b[-1][:dof].copy_(torch.tensor([0.1, -0.2, 0.05, 0.3, -0.1][:dof]))
+    s.export_weights()
+    return s
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('dims,dof', [((8, 6, 1), 3), ((5, 4, 3), 4), ((70, 20, 1), 3)])
+def test_gradients_match_cpu_autograd(dims, dof):
+    """Loss and the gradient of every weight and bias through the GPU
+    backward kernels against CPU autograd of the oracle network.  The GPU
+    path rounds the back-propagated gradient to BF16 before each
+    transposed convolution; the oracle keeps it in FP32, hence 2e-2 on the
+    relative norm of each gradient."""
+    s = _surrogate(dof, seed=3)
+    ncell = dims[0] * dims[1] * dims[2]
+    g = torch.Generator().manual_seed(4)
+    x = torch.randn(ncell * dof, generator=g, dtype=torch.float64).cuda()
+    t = torch.randn(ncell * dof, generator=g, dtype=torch.float64).cuda()
+    x1 = x + 0.3 * t + 0.01 * torch.randn(ncell * dof, generator=g, dtype=torch.float64).cuda()
+    sample = {'x0': x, 't': t, 'mu': 250.0, 'ds': 0.3, 'x1': x1}
+    s.fit_scales([sample])
+    b = s._buffers(dims)
+    s._pack(b, x, t, sample['mu'], sample['ds'])
+    s._target(b, sample)
+    s._forward(b)
+    s._backward(b, ctypes.c_void_p(b['loss'].data_ptr()), False)
+    torch.cuda.synchronize()
+    # the packed input, exactly: scaled fields, then mu and ds
+    x0 = b['x0'].view(ncell, s.kp[0]).float().cpu()
+    sc = s.scales
+    want = torch.zeros(ncell, s.kp[0])
+    want[:, :dof] = (x.view(ncell, dof).float().cpu() * torch.tensor(sc['sx']).float())
+    want[:, dof:2 * dof] = (t.view(ncell, dof).float().cpu() * torch.tensor(sc['st']).float())
+    want[:, 2 * dof] = float(np.float32(sample['mu'] * sc['mu']))
+    want[:, 2 * dof + 1] = float(np.float32(sample['ds'] * sc['ds']))
+    assert torch.equal(x0, ref.bf16(want))
+    tgt = b['tgt'].view(ncell, dof).cpu()
+    loss, gw, gb = ref.loss_and_grads(x0, tgt, [w.cpu() for w in s.w], [bb.cpu() for bb in s.b], dims, dof)
+    assert abs(float(b['loss'].item()) - loss) <= 1e-4 * loss
+    for layer in range(s.layers):
+        gr = s.grad[layer].view(28, s.kp[layer], s.np[layer]).cpu()
+        e_w = (gr[:27] - gw[layer]).norm() / gw[layer].norm()
+        e_b = (gr[27, 0] - gb[layer]).norm() / max(gb[layer].norm(), 1e-30)
+        assert e_w <= 2e-2, (layer, float(e_w))
+        assert e_b <= 2e-2, (layer, float(e_b))
+
+
+@pytest.mark.gpu
+def test_adam_step_and_weight_layouts():
+    """One Adam step against its formula, and both BF16 layouts the
+    convolutions read (forward [tap][co][ci], backward-data the mirrored tap
+    [26 - tap][ci][co]) written from the updated master weights."""
+    s = _surrogate(3, seed=5, layers=2)
+    g = torch.Generator().manual_seed(6)
+    w0 = [w.cpu().clone() for w in s.w]
+    b0 = [b.cpu().clone() for b in s.b]
+    grads = []
+    for layer in range(2):
+        gr = torch.randn(28, s.kp[layer], s.np[layer], generator=g)
+        s.grad[layer].copy_(gr.view(-1))
+        grads.append(gr * 0.5)
+    s._adam(1e-2, 2)
+    torch.cuda.synchronize()
+    for layer in range(2):
+        gr = grads[layer]
+        upd = lambda p, gg: p - 1e-2 * ((0.1 * gg) / 0.1) / (torch.sqrt((0.001 * gg * gg) / 0.001) + 1e-8)
+        w1 = upd(w0[layer], gr[:27])
+        b1 = upd(b0[layer], gr[27, 0])
+        assert torch.allclose(s.w[layer].cpu(), w1, rtol=1e-5, atol=1e-6)
+        assert torch.allclose(s.b[layer].cpu(), b1, rtol=1e-5, atol=1e-6)
+        wq = s.w[layer].cpu().to(torch.bfloat16)
+        kp, np_ = s.kp[layer], s.np[layer]
+        assert torch.equal(s.wf[layer].view(27, np_, kp).cpu(), wq.permute(0, 2, 1))
+        assert torch.equal(s.wb[layer].view(27, kp, np_).cpu(), wq.flip(0))
+
+
+def _branch_samples():
+    from transiflow_gb300 import Interface
+    from transiflow_gb300.continuation import Continuation
+    from transiflow_gb300.surrogate import Recorder
+    itf = Interface({}, 16, 16)
+    rec = Recorder()
+    cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=rec.predictor, log=rec.log)
+    x0 = cont.newton(itf.vector())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x, mu = cont.continuation(x0.copy(), 'Reynolds Number', 0, 2000, 100)
+    torch.cuda.synchronize()
+    stats = dict(cont.stats, wall_s=time.perf_counter() - t0)
+    return itf, x0, x, stats, rec.samples
+
+
+@pytest.fixture(scope='module')
+def trained():
+    if not torch.cuda.is_available():
+        pytest.skip('needs a GPU')
+    from transiflow_gb300.surrogate import Surrogate
+    itf, x0, x_plain, stats, samples = _branch_samples()
+    s = Surrogate(itf.dof, seed=0)
+    s.fit_scales(samples)
+    before = s.evaluate(samples, (16, 16, 1))
+    losses = s.train(samples, (16, 16, 1), steps=400, lr=2e-3, batch=4)
+    after = s.evaluate(samples, (16, 16, 1))
+    return {'itf': itf, 'x0': x0, 'x_plain': x_plain, 'stats': stats, 'samples': samples, 's': s,
+            'before': before, 'after': after, 'losses': losses}
+
+
+@pytest.mark.gpu
+def test_training_reduces_the_predictor_error(trained):
+    """Trained on the branch points of a plain continuation (2D lid-driven
+    cavity 16x16, Re 0 -> 2000, ds = 100), the network's predictor is
+    closer to the corrected points than the secant predictor it starts
+    from.  The scaled error of the untrained network is the secant
+    predictor's (about 1 by construction)."""
+    before, after = trained['before'], trained['after']
+    print('samples %d, secant error %.4f, learned error %.4f, final training loss %.4f'
+          % (len(trained['samples']), before.mean(), after.mean(), trained['losses'][-10:].mean()))
+    assert len(trained['samples']) >= 8
+    assert np.all(np.isfinite(after))
+    assert after.mean() < 0.8 * before.mean()
+
+
+@pytest.mark.gpu
+def test_learned_continuation_reaches_the_same_branch_end(trained):
+    """Continuation with the learned predictor reaches Re = 2000 at the same
+    solution as the plain run (both polished by Newton to ||F|| <= 1e-12),
+    every accepted point has ||F|| <= 1e-8, and the learned predictions are
+    used.  The solve counts of both runs are printed: the gain of the
+    network over the secant predictor on this branch."""
+    from transiflow_gb300.continuation import Continuation
+    from transiflow_gb300.surrogate import LearnedPredictor
+    itf = trained['itf']
+    itf.set_parameter('Reynolds Number', 0)
+    fn = []
+    cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=LearnedPredictor(trained['s']),
+                        log=lambda r: fn.append(r['fnorm']))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x, mu = cont.continuation(trained['x0'].copy(), 'Reynolds Number', 0, 2000, 100)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    assert abs(mu - 2000) < 1e-3
+    assert all(f is not None and f <= 1e-8 for f in fn)
+    assert cont.stats['learned_accepted'] > 0
+    print('plain: %s\nlearned: %s, wall_s %.3f' % (trained['stats'], cont.stats, wall))
+    itf.set_parameter('Reynolds Number', 2000)
+    polish = Continuation(itf, quiet=True)
+    xa = polish.newton(x, 1e-12).numpy()
+    xb = polish.newton(trained['x_plain'], 1e-12).numpy()
+    assert np.linalg.norm(xa - xb) <= 1e-8 * np.linalg.norm(xb)

@@ -24,7 +24,7 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 SOURCES = [('tf_assemble.cu', ['-fmad=false']), ('tf_sparse.cu', []), ('tf_nd.cu', []), ('tf_nd_panel_f32.cu', []),
            ('tf_nd_panel_f64.cu', []),
            ('tf_nd_inv.cu', []), ('tf_nd_flow.cu', []),
-           ('tf_nd_sweep.cu', [])]
+           ('tf_nd_sweep.cu', []), ('tf_surrogate.cu', [])]
 
 TF_MAX_BC_OPS = 24
 TF_METRIC_FIELDS = 10
@@ -149,6 +149,17 @@ _SIGNATURES = {
     'tf_nd_solve_sweep_f64': ([_P, _P, _P, _P, _P, ctypes.c_size_t, _I, _P], _I),
     'tf_nd_solve_sweep_f32': ([_P, _P, _P, _P, _P, ctypes.c_size_t, _I, _P], _I),
     'tf_nd_sweep_status': ([_P], _I),
+    'tf_sg_conv': ([_I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _I, _P], _I),
+    'tf_sg_wgrad_workspace_bytes': ([_I, _I, _I], ctypes.c_size_t),
+    'tf_sg_wgrad': ([_I, _I, _I, _I, _I, _P, _P, _P, _I, _P, ctypes.c_size_t, _P], _I),
+    'tf_sg_loss_workspace_bytes': ([_I, _I], ctypes.c_size_t),
+    'tf_sg_loss': ([_I, _I, _I, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
+    'tf_sg_act_grad': ([ctypes.c_longlong, _P, _P, _P, _P, _P], _I),
+    'tf_sg_pack': ([_I, _I, _I, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P], _I),
+    'tf_sg_target': ([_I, _I, _P, _P, _P, _D, _P, _P, _P], _I),
+    'tf_sg_unpack': ([_I, _I, _I, _P, _P, _P, _D, _P, _P, _P], _I),
+    'tf_sg_adam': ([_I, _I, _P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                    _I, ctypes.c_float, _P, _P, _P], _I),
 }
 
 _lib = None

@@ -14,9 +14,11 @@ Vectors may be NumPy arrays or :class:`transiflow_gb300.vector.DeviceVector`;
 both support ``x.size``, ``.dot``, ``.T.conj() @ y`` and scalar arithmetic.
 
 Beyond the reference: an optional ``predictor`` callable can propose the
-continuation predictor (the learned surrogate plugs in here); the secant
-predictor of the reference is used whenever it is absent or its corrector
-fails, and every accepted point is judged by the same Newton corrector.  An
+continuation predictor (the learned surrogate of
+:mod:`transiflow_gb300.surrogate` plugs in here); the secant predictor of the
+reference is used whenever it is absent or its corrector does not converge
+within ``learned_newton_iterations`` iterations, and every accepted point is
+judged by the same Newton corrector.  An
 optional ``log`` callable receives one dict per accepted point.
 """
 
@@ -51,7 +53,8 @@ class Continuation:
     def __init__(self, interface, delta=1.0, destination_tolerance=1e-4,
                  newton_tolerance=1e-4, maximum_newton_iterations=10,
                  optimal_newton_iterations=3, residual_check='F',
-                 bordered_solver=False, verbose=False, predictor=None, log=None, quiet=False):
+                 bordered_solver=False, verbose=False, predictor=None, log=None, quiet=False,
+                 learned_newton_iterations=4):
         self.interface = interface
         self.quiet = quiet
         self.verbose = verbose
@@ -65,6 +68,7 @@ class Continuation:
         self.residual_check = residual_check
         self.bordered_solver = bordered_solver
         self.predictor = predictor
+        self.learned_newton_iterations = learned_newton_iterations
         self.log = log
         self.stats = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'points': 0,
                       'failed_correctors': 0, 'learned_accepted': 0, 'learned_rejected': 0}
@@ -114,12 +118,13 @@ class Continuation:
         return x
 
     # -- corrector (Continuation.py:116-195) ----------------------------------
-    def _newton_corrector(self, name, ds, x, x0, mu, mu0):
+    def _newton_corrector(self, name, ds, x, x0, mu, mu0, maxit=None):
+        maxit = self.maximum_newton_iterations if maxit is None else maxit
         self.newton_iterations = 0
         fnorm = None
         dxnorm = None
         self._last_fnorm = None
-        for k in range(self.maximum_newton_iterations):
+        for k in range(maxit):
             self.interface.set_parameter(name, mu)
             fval = self._rhs(x)
             if self.residual_check == 'F' or self.verbose:
@@ -130,7 +135,7 @@ class Continuation:
                 self._say('Newton corrector converged in %d iterations with ||F||=%e' % (k, fnorm), flush=True)
                 break
             if self.residual_check == 'F' and prev_norm is not None and prev_norm < fnorm:
-                self.newton_iterations = self.maximum_newton_iterations
+                self.newton_iterations = maxit
                 break
             diff = x - x0
             rnp1 = self.zeta * diff.dot(diff) + (1 - self.zeta) * (mu - mu0) ** 2 - ds ** 2
@@ -159,9 +164,9 @@ class Continuation:
             if self.verbose:
                 self._say('Newton corrector status at iteration %d: ||F||=%e, ||dx||=%e' % (k, fnorm, dxnorm), flush=True)
             if self.residual_check != 'F' and prev_norm is not None and prev_norm < dxnorm:
-                self.newton_iterations = self.maximum_newton_iterations
+                self.newton_iterations = maxit
                 break
-        if self.newton_iterations == self.maximum_newton_iterations:
+        if self.newton_iterations == maxit:
             self._say('Newton did not converge. Adjusting step size and trying again', flush=True)
             self.stats['failed_correctors'] += 1
             return x0, mu0
@@ -201,7 +206,8 @@ class Continuation:
         else:
             mu = mu0 + ds * dmu
             x = x0 + ds * dx
-        x, mu = self._newton_corrector(name, ds, x, x0, mu, mu0)
+        x, mu = self._newton_corrector(name, ds, x, x0, mu, mu0,
+                                       self.learned_newton_iterations if learned is not None else None)
         if learned is not None:
             if mu == mu0:
                 # The learned predictor failed: fall back to the secant predictor.

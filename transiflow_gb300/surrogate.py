@@ -1,0 +1,293 @@
+"""Learned continuation predictor: a convolutional surrogate trained on the
+branch points that plain continuation computes.
+
+The network reads the current state ``x``, the secant tangent ``t``, the
+parameter ``mu`` and the step ``ds`` on the cell grid and proposes the
+correction to the secant predictor ``x + ds*t``.  The Newton corrector of the
+continuation judges every point; the secant predictor is the fallback
+whenever the corrector started from the learned predictor does not converge
+within ``Continuation(learned_newton_iterations=4)`` iterations.
+
+Architecture: ``layers`` 3x3x3 convolutions over the cell grid (a 2D grid is
+a grid one cell thick), ``channels`` channels between them, ReLU after every
+layer but the last.  Inputs are ``2*dof + 2`` channels (x and t per
+variable, mu and ds as constant fields), outputs ``dof`` channels.  Forward,
+backward and Adam run in libtfcuda kernels (``tf_sg_*``): BF16 operands with
+FP32 accumulation on the tensor cores, FP32 master weights.  Inputs and
+targets are scaled per variable with statistics of the training samples; the
+target is the corrector's displacement from the secant predictor divided by
+``ds**2`` (the order of the secant predictor's error), so the zero-initialised
+last layer starts the network at exactly the secant predictor.
+
+The reference has no counterpart: its continuation predicts with the secant
+only (transiflow/Continuation.py:258-260).
+"""
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .vector import DeviceVector, _stream
+
+__all__ = ['Surrogate', 'Recorder', 'LearnedPredictor']
+
+
+def _pad16(c):
+    return 16 if c <= 16 else 32
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class Recorder:
+    """Collects training samples from a plain continuation: pass
+    ``recorder.predictor`` as the continuation's predictor (it proposes
+    nothing, so the secant predictor runs) and ``recorder.log`` as its log.
+    A sample is (x0, t, mu0, ds, x1): the state, tangent and parameter a
+    step started from, the step it was accepted with and the point it
+    converged to."""
+
+    def __init__(self):
+        self.samples = []
+        self._pending = None
+        self._ds = None
+
+    def predictor(self, interface, x0, mu0, dx, dmu, ds):
+        if self._pending is not None and self._ds is not None:
+            px, pt, pmu = self._pending
+            self.samples.append({'x0': px, 't': pt, 'mu': pmu, 'ds': self._ds, 'x1': x0.data.clone()})
+        self._pending = (x0.data.clone(), dx.data.clone(), float(mu0))
+        self._ds = None
+        return None
+
+    def log(self, record):
+        self._ds = float(record['ds'])
+
+
+class Surrogate:
+    """The network, its Adam state and its scratch buffers (per grid shape)."""
+
+    def __init__(self, dof, channels=32, layers=4, seed=0, device=None):
+        if channels not in (16, 32):
+            raise ValueError('channels must be 16 or 32')
+        if layers < 2:
+            raise ValueError('the surrogate needs at least two layers')
+        if 2 * dof + 2 > 32:
+            raise ValueError('at most 15 variables per cell')
+        self.lib = _lib.load()
+        self.device = torch.device(device or 'cuda')
+        self.dof = dof
+        self.layers = layers
+        cin = 2 * dof + 2
+        self.kp = [_pad16(cin)] + [channels] * (layers - 1)
+        self.np = [channels] * (layers - 1) + [_pad16(dof)]
+        real_in = [cin] + [channels] * (layers - 1)
+        real_out = [channels] * (layers - 1) + [dof]
+        gen = torch.Generator().manual_seed(seed)
+        self.w, self.b, self.grad, self.m, self.v, self.wf, self.wb = [], [], [], [], [], [], []
+        for layer in range(layers):
+            kp, np_ = self.kp[layer], self.np[layer]
+            w = torch.zeros(27, kp, np_, dtype=torch.float32)
+            if layer < layers - 1:
+                # He-uniform for the ReLU layers; the last layer starts at zero
+                bound = math.sqrt(6.0 / (27 * real_in[layer]))
+                w[:, :real_in[layer], :real_out[layer]] = \
+                    (torch.rand(27, real_in[layer], real_out[layer], generator=gen) * 2 - 1) * bound
+            dev = dict(device=self.device)
+            self.w.append(w.to(self.device).contiguous())
+            self.b.append(torch.zeros(np_, dtype=torch.float32, **dev))
+            for lst in (self.grad, self.m, self.v):
+                lst.append(torch.zeros(28 * kp * np_, dtype=torch.float32, **dev))
+            self.wf.append(torch.empty(27 * np_ * kp, dtype=torch.bfloat16, **dev))
+            self.wb.append(torch.empty(27 * kp * np_, dtype=torch.bfloat16, **dev))
+        self.step = 0
+        self.scales = None
+        self._bufs = {}
+        self.export_weights()
+
+    # -- weights ----------------------------------------------------------------
+    def export_weights(self):
+        """Write both BF16 layouts of every layer from the master weights
+        (after construction or an edit of ``w`` / ``b``)."""
+        s = _stream()
+        for layer in range(self.layers):
+            _lib.check(self.lib.tf_sg_adam(self.kp[layer], self.np[layer], _ptr(self.w[layer]), _ptr(self.b[layer]),
+                                           None, None, None, 0.0, 0.0, 0.0, 0.0, 0, 1.0,
+                                           _ptr(self.wf[layer]), _ptr(self.wb[layer]), s), 'tf_sg_adam')
+
+    def parameters(self):
+        return sum(int(w.numel()) + int(b.numel()) for w, b in zip(self.w, self.b))
+
+    # -- scratch ------------------------------------------------------------------
+    def _buffers(self, dims):
+        dims = tuple(int(d) for d in dims)
+        if dims in self._bufs:
+            return self._bufs[dims]
+        nx, ny, nz = dims
+        ncell = nx * ny * nz
+        dev = dict(device=self.device)
+        L = self.layers
+        b = {'dims': dims, 'ncell': ncell,
+             'x0': torch.empty(ncell * self.kp[0], dtype=torch.bfloat16, **dev),
+             'z': [torch.empty(ncell * n, dtype=torch.float32, **dev) for n in self.np],
+             'a': [torch.empty(ncell * n, dtype=torch.bfloat16, **dev) for n in self.np[:L - 1]],
+             'dzf': [torch.empty(ncell * n, dtype=torch.float32, **dev) for n in self.np],
+             'dzh': [torch.empty(ncell * n, dtype=torch.bfloat16, **dev) for n in self.np],
+             'da': [torch.empty(ncell * n, dtype=torch.float32, **dev) for n in self.np[:L - 1]],
+             'tgt': torch.empty(ncell * self.dof, dtype=torch.float32, **dev),
+             'loss': torch.zeros(1, dtype=torch.float64, **dev)}
+        lw = self.lib.tf_sg_loss_workspace_bytes(ncell, self.np[-1])
+        ww = max(self.lib.tf_sg_wgrad_workspace_bytes(ncell, kp, np_) for kp, np_ in zip(self.kp, self.np))
+        b['lwork'] = torch.empty(lw, dtype=torch.uint8, **dev)
+        b['wwork'] = torch.empty(ww, dtype=torch.uint8, **dev)
+        self._bufs[dims] = b
+        return b
+
+    # -- the kernels in order ------------------------------------------------------
+    def _pack(self, b, x, t, mu, ds):
+        sc = self.scales
+        sx = (ctypes.c_float * self.dof)(*sc['sx'])
+        st = (ctypes.c_float * self.dof)(*sc['st'])
+        _lib.check(self.lib.tf_sg_pack(b['ncell'], self.dof, self.kp[0], _ptr(x), _ptr(t), sx, st,
+                                       float(mu * sc['mu']), float(ds * sc['ds']), _ptr(b['x0']), _stream()),
+                   'tf_sg_pack')
+
+    def _target(self, b, sample):
+        ds = sample['ds']
+        inv = (ctypes.c_double * self.dof)(*[1.0 / (ds * ds * s) for s in self.scales['sd']])
+        _lib.check(self.lib.tf_sg_target(b['ncell'], self.dof, _ptr(sample['x0']), _ptr(sample['t']),
+                                         _ptr(sample['x1']), float(ds), inv, _ptr(b['tgt']), _stream()),
+                   'tf_sg_target')
+
+    def _forward(self, b):
+        nx, ny, nz = b['dims']
+        s = _stream()
+        inp = b['x0']
+        for layer in range(self.layers):
+            last = layer == self.layers - 1
+            _lib.check(self.lib.tf_sg_conv(nx, ny, nz, self.kp[layer], self.np[layer], _ptr(inp),
+                                           _ptr(self.wf[layer]), _ptr(self.b[layer]), _ptr(b['z'][layer]),
+                                           None if last else _ptr(b['a'][layer]), 0 if last else 1, s),
+                       'tf_sg_conv')
+            if not last:
+                inp = b['a'][layer]
+
+    def _backward(self, b, loss_ptr, accumulate):
+        nx, ny, nz = b['dims']
+        ncell = b['ncell']
+        s = _stream()
+        L = self.layers
+        _lib.check(self.lib.tf_sg_loss(ncell, self.dof, self.np[-1], _ptr(b['z'][-1]), _ptr(b['tgt']),
+                                       _ptr(b['dzf'][-1]), _ptr(b['dzh'][-1]), loss_ptr,
+                                       _ptr(b['lwork']), b['lwork'].numel(), s), 'tf_sg_loss')
+        for layer in range(L - 1, -1, -1):
+            inp = b['x0'] if layer == 0 else b['a'][layer - 1]
+            _lib.check(self.lib.tf_sg_wgrad(nx, ny, nz, self.kp[layer], self.np[layer], _ptr(inp),
+                                            _ptr(b['dzf'][layer]), _ptr(self.grad[layer]), 1 if accumulate else 0,
+                                            _ptr(b['wwork']), b['wwork'].numel(), s), 'tf_sg_wgrad')
+            if layer > 0:
+                # gradient with respect to the layer's input: the same
+                # convolution over dZ with the mirrored, transposed weights
+                _lib.check(self.lib.tf_sg_conv(nx, ny, nz, self.np[layer], self.kp[layer], _ptr(b['dzh'][layer]),
+                                               _ptr(self.wb[layer]), None, _ptr(b['da'][layer - 1]), None, 0, s),
+                           'tf_sg_conv')
+                _lib.check(self.lib.tf_sg_act_grad(ncell * self.np[layer - 1], _ptr(b['da'][layer - 1]),
+                                                   _ptr(b['z'][layer - 1]), _ptr(b['dzf'][layer - 1]),
+                                                   _ptr(b['dzh'][layer - 1]), s), 'tf_sg_act_grad')
+
+    def _adam(self, lr, batch):
+        self.step += 1
+        s = _stream()
+        for layer in range(self.layers):
+            _lib.check(self.lib.tf_sg_adam(self.kp[layer], self.np[layer], _ptr(self.w[layer]), _ptr(self.b[layer]),
+                                           _ptr(self.grad[layer]), _ptr(self.m[layer]), _ptr(self.v[layer]),
+                                           float(lr), 0.9, 0.999, 1e-8, self.step, 1.0 / batch,
+                                           _ptr(self.wf[layer]), _ptr(self.wb[layer]), s), 'tf_sg_adam')
+
+    # -- training -----------------------------------------------------------------
+    def fit_scales(self, samples):
+        """Per-variable input and target scales from the training samples."""
+        dof = self.dof
+
+        def rms(vs):
+            a = torch.stack([v.view(-1, dof) for v in vs]).pow(2).mean(dim=(0, 1)).sqrt().cpu().numpy()
+            return [float(v) if v > 1e-300 else 1.0 for v in a]
+        xr = rms([s['x0'] for s in samples])
+        tr = rms([s['t'] for s in samples])
+        dr = rms([(s['x1'] - s['x0'] - s['ds'] * s['t']) / (s['ds'] ** 2) for s in samples])
+        mu = max(abs(s['mu']) for s in samples) or 1.0
+        ds = max(abs(s['ds']) for s in samples) or 1.0
+        self.scales = {'sx': [1.0 / v for v in xr], 'st': [1.0 / v for v in tr], 'sd': dr,
+                       'mu': 1.0 / mu, 'ds': 1.0 / ds}
+
+    def train(self, samples, dims, steps=300, lr=1e-3, batch=4, seed=0):
+        """Adam on the mean-squared scaled target; returns the loss per step
+        (mean over its batch), read back once at the end."""
+        if not samples:
+            raise ValueError('no training samples')
+        if self.scales is None:
+            self.fit_scales(samples)
+        b = self._buffers(dims)
+        rng = np.random.default_rng(seed)
+        batch = min(batch, len(samples))
+        losses = torch.zeros(steps * batch, dtype=torch.float64, device=self.device)
+        for it in range(steps):
+            for j, i in enumerate(rng.choice(len(samples), size=batch, replace=False)):
+                sample = samples[i]
+                self._pack(b, sample['x0'], sample['t'], sample['mu'], sample['ds'])
+                self._target(b, sample)
+                self._forward(b)
+                self._backward(b, ctypes.c_void_p(losses.data_ptr() + 8 * (it * batch + j)), j > 0)
+            self._adam(lr, batch)
+        return losses.view(steps, batch).mean(dim=1).cpu().numpy()
+
+    def evaluate(self, samples, dims):
+        """Scaled mean-squared error of the predictor per sample (1.0 is the
+        secant predictor's error level)."""
+        if self.scales is None:
+            raise RuntimeError('fit_scales() or train() sets the scales first')
+        b = self._buffers(dims)
+        out = torch.zeros(len(samples), dtype=torch.float64, device=self.device)
+        for k, sample in enumerate(samples):
+            self._pack(b, sample['x0'], sample['t'], sample['mu'], sample['ds'])
+            self._target(b, sample)
+            self._forward(b)
+            _lib.check(self.lib.tf_sg_loss(b['ncell'], self.dof, self.np[-1], _ptr(b['z'][-1]), _ptr(b['tgt']),
+                                           _ptr(b['dzf'][-1]), _ptr(b['dzh'][-1]),
+                                           ctypes.c_void_p(out.data_ptr() + 8 * k), _ptr(b['lwork']),
+                                           b['lwork'].numel(), _stream()), 'tf_sg_loss')
+        return out.cpu().numpy()
+
+    # -- inference ------------------------------------------------------------------
+    def predict(self, x, t, mu, ds, dims):
+        """The learned predictor x + ds t + correction (FP64 tensor)."""
+        if self.scales is None:
+            raise RuntimeError('the surrogate has not been trained')
+        b = self._buffers(dims)
+        self._pack(b, x, t, mu, ds)
+        self._forward(b)
+        xp = torch.empty_like(x)
+        sc = (ctypes.c_double * self.dof)(*[ds * ds * s for s in self.scales['sd']])
+        _lib.check(self.lib.tf_sg_unpack(b['ncell'], self.dof, self.np[-1], _ptr(b['z'][-1]), _ptr(x), _ptr(t),
+                                         float(ds), sc, _ptr(xp), _stream()), 'tf_sg_unpack')
+        return xp
+
+
+class LearnedPredictor:
+    """The continuation's ``predictor`` hook over a trained surrogate: the
+    state from the network, the parameter from the secant."""
+
+    def __init__(self, surrogate):
+        self.surrogate = surrogate
+        self.calls = 0
+
+    def __call__(self, interface, x0, mu0, dx, dmu, ds):
+        if self.surrogate.scales is None:
+            return None
+        self.calls += 1
+        xp = self.surrogate.predict(x0.data, dx.data, mu0, ds, (interface.nx, interface.ny, interface.nz))
+        return DeviceVector(xp), mu0 + ds * dmu
