@@ -84,6 +84,37 @@ def test_continuation_falls_back_to_the_secant_predictor(quality):
         assert cont.stats['learned_accepted'] == 0 and cont.stats['learned_rejected'] > 0
 
 
+def test_recorder_collects_consecutive_steps():
+    """Recorder samples from a plain continuation: each sample's corrected
+    point is the next sample's start, its step is the one the step was
+    accepted with, and the secant predictor runs unchanged (same branch as
+    a run without the recorder)."""
+    from transiflow_gb300.continuation import Continuation
+    from transiflow_gb300.surrogate import Recorder
+    itf = _Cubic()
+    plain = Continuation(itf, newton_tolerance=1e-10, quiet=True)
+    xp, mup = plain.continuation(np.zeros(2), 'mu', 0.0, 10.0, 0.5)
+    itf = _Cubic()
+    rec = Recorder()
+    steps = []
+    cont = Continuation(itf, newton_tolerance=1e-10, quiet=True, predictor=rec.predictor,
+                        log=lambda r: (steps.append(r), rec.log(r)))
+    x, mu = cont.continuation(np.zeros(2), 'mu', 0.0, 10.0, 0.5)
+    assert mu == mup and np.array_equal(x, xp)
+    assert cont.stats['points'] == plain.stats['points']
+    smp = rec.samples
+    assert len(smp) >= 3
+    for a, b in zip(smp, smp[1:]):
+        assert torch.equal(a['x1'], b['x0'])
+    for k, sm in enumerate(smp):
+        assert sm['ds'] == steps[k]['ds']
+        # the tangent is the normalised secant of the previous step
+        x1 = sm['x0'].numpy() + sm['ds'] * sm['t'].numpy()
+        assert np.all(np.isfinite(x1))
+        r = np.roots([1, 0, 1, -sm['mu']]).real.max()
+        assert np.allclose(sm['x0'].numpy(), [r, 0.5 * sm['mu']], rtol=1e-9, atol=1e-9)
+
+
 # -- GPU: the kernels against the oracle ---------------------------------------
 
 def _lib():

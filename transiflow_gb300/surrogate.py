@@ -43,6 +43,13 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+def _snapshot(v):
+    """A copy of a continuation vector as a tensor (DeviceVector or NumPy)."""
+    if isinstance(v, DeviceVector):
+        return v.data.clone()
+    return torch.tensor(np.asarray(v, dtype=np.float64))
+
+
 class Recorder:
     """Collects training samples from a plain continuation: pass
     ``recorder.predictor`` as the continuation's predictor (it proposes
@@ -59,8 +66,8 @@ class Recorder:
     def predictor(self, interface, x0, mu0, dx, dmu, ds):
         if self._pending is not None and self._ds is not None:
             px, pt, pmu = self._pending
-            self.samples.append({'x0': px, 't': pt, 'mu': pmu, 'ds': self._ds, 'x1': x0.data.clone()})
-        self._pending = (x0.data.clone(), dx.data.clone(), float(mu0))
+            self.samples.append({'x0': px, 't': pt, 'mu': pmu, 'ds': self._ds, 'x1': _snapshot(x0)})
+        self._pending = (_snapshot(x0), _snapshot(dx), float(mu0))
         self._ds = None
         return None
 
