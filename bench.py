@@ -435,7 +435,7 @@ def reference_arm(args, rank):
         t = oracle_sample(args.nx)
         vals.append(extrapolate(t, calls))
     v = statistics.mean(vals)
-    return {'metric': METRIC, 'value': v, 'unit': 's', 'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+    return {'metric': METRIC, 'value': v, 'unit': 's', 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
             'ms_per_step': v * 1000.0, 'higher_is_better': False, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference', 'config': config(args),
             'cpu_baseline': {'value': v, 'unit': 's', 'cores': 1, 'kind': 'port',
