@@ -70,6 +70,14 @@ def parse():
     ap.add_argument('--reuse-its', type=int, default=None, help="'Reuse Iterations' (default: the backend's)")
     ap.add_argument('--no-inverse', action='store_true', help="'Inverse Apply': False (substitution solves)")
     ap.add_argument('--reuse-drift', type=float, default=None, help="'Reuse Drift' (default: the backend's)")
+    ap.add_argument('--learned', action='store_true',
+                    help='train the learned predictor on plain branches of the --train-grids, then time the '
+                         'branch at --nx/--nz plain (FP64 factors) and learned (FP32 factors), then exit')
+    ap.add_argument('--train-grids', default='32,48', help='--learned: training grid sizes (cubes when --nz > 1)')
+    ap.add_argument('--train-seeds', default='3,4,5,6', help='--learned: one training branch per seed and grid')
+    ap.add_argument('--train-target', type=float, default=2500.0, help='--learned: Re at the end of training branches')
+    ap.add_argument('--train-steps', type=int, default=100, help='--learned: Adam steps per grid and round')
+    ap.add_argument('--train-rounds', type=int, default=4, help='--learned: rounds over the training grids')
     ap.add_argument('--sweep-heights', type=int, default=0,
                     help='with --apply sweep: tree heights nearest the root in the cooperative launch (0: all)')
     return ap.parse_args()
@@ -517,6 +525,83 @@ def batched(args):
                       'unknowns': int(sum(3 * s['nx'] ** 2 for s in specs))}))
 
 
+def learned(args):
+    """The learned + mixed configuration against plain FP64 on one GPU.
+    Training: one plain FP64 branch (Re 0 -> --train-target, ||F|| <= 1e-8)
+    per training grid and seed, the seed drawing the initial step from
+    [0.5, 1.5] x --ds; the learned predictor is trained on all their points
+    (Adam, --train-rounds rounds of --train-steps steps per grid).  Timed:
+    Newton at Re = 0 and the branch to --target at --nx/--nz, plain (secant
+    predictor, FP64 factors) and learned (learned predictor, FP32 factors),
+    each after a short warm-up branch on the same grid; every point at
+    ||F|| <= 1e-8, the end points compared after Newton polishing at the
+    target."""
+    import torch
+    from transiflow_gb300 import Continuation, Interface
+    from transiflow_gb300.surrogate import LearnedPredictor, Recorder, Surrogate
+    three_d = args.nz > 1
+
+    def make(n, precision):
+        return Interface({'CUDA': {'Factor Precision': precision, 'Tolerance': args.tol}},
+                         n, n, n if three_d else 1)
+
+    t0 = time.perf_counter()
+    groups = []
+    for n in [int(v) for v in args.train_grids.split(',')]:
+        for seed in [int(v) for v in args.train_seeds.split(',')]:
+            itf = make(n, 'fp64')
+            rec = Recorder()
+            cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=rec.predictor, log=rec.log)
+            itf.set_parameter('Reynolds Number', 0.0)
+            x0 = cont.newton(itf.vector())
+            ds = args.ds * float(np.random.default_rng(seed).uniform(0.5, 1.5))
+            cont.continuation(x0, 'Reynolds Number', 0.0, args.train_target, ds)
+            groups.append(((n, n, n if three_d else 1), rec.samples))
+    branches_s = time.perf_counter() - t0
+    net = Surrogate(4 if three_d else 3)
+    net.fit_scales([smp for _, g in groups for smp in g])
+    t1 = time.perf_counter()
+    for r in range(args.train_rounds):
+        for dims, g in groups:
+            if g:
+                net.train(g, dims, steps=args.train_steps, lr=2e-3, batch=4, seed=r)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+
+    def branch(precision, predictor):
+        itf = make(args.nx, precision)
+        fn = []
+        cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=predictor,
+                            log=lambda rec: fn.append(rec['fnorm']))
+        itf.set_parameter('Reynolds Number', 0.0)
+        cont.continuation(cont.newton(itf.vector()), 'Reynolds Number', 0.0, min(args.target, 2 * args.ds),
+                          args.ds)                                  # warm-up: plans, graphs
+        itf.set_parameter('Reynolds Number', 0.0)
+        fn.clear()
+        cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=predictor,
+                            log=lambda rec: fn.append(rec['fnorm']))
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        x = cont.newton(itf.vector())
+        x, mu = cont.continuation(x, 'Reynolds Number', 0.0, args.target, args.ds)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t
+        itf.set_parameter('Reynolds Number', args.target)
+        xp = Continuation(itf, quiet=True).newton(x, 1e-12).numpy()
+        return wall, dict(cont.stats), max(f for f in fn if f is not None), xp
+
+    plain_s, plain_stats, plain_f, xa = branch('fp64', None)
+    learned_s, learned_stats, learned_f, xb = branch('fp32', LearnedPredictor(net))
+    print(json.dumps({'learned': True, 'nx': args.nx, 'nz': args.nz, 'target_re': args.target, 'ds': args.ds,
+                      'plain_fp64_s': plain_s, 'learned_mixed_s': learned_s, 'speedup': plain_s / learned_s,
+                      'plain_stats': plain_stats, 'learned_stats': learned_stats,
+                      'max_fnorm': max(plain_f, learned_f),
+                      'end_point_rel_diff': float(np.linalg.norm(xb - xa) / np.linalg.norm(xa)),
+                      'train_grids': args.train_grids, 'train_seeds': args.train_seeds,
+                      'train_samples': sum(len(g) for _, g in groups), 'train_branches_s': branches_s,
+                      'train_s': train_s, 'parameters': net.parameters()}))
+
+
 def main():
     args = parse()
     if args.profile:
@@ -524,6 +609,9 @@ def main():
         return
     if args.batched:
         batched(args)
+        return
+    if args.learned:
+        learned(args)
         return
     from transiflow_gb300 import dist
     rank, world, local = dist.init_from_env()

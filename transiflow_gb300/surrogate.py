@@ -221,7 +221,8 @@ class Surrogate:
         dof = self.dof
 
         def rms(vs):
-            a = torch.stack([v.view(-1, dof) for v in vs]).pow(2).mean(dim=(0, 1)).sqrt().cpu().numpy()
+            # samples may come from grids of different sizes
+            a = torch.cat([v.view(-1, dof) for v in vs]).pow(2).mean(dim=0).sqrt().cpu().numpy()
             return [float(v) if v > 1e-300 else 1.0 for v in a]
         xr = rms([s['x0'] for s in samples])
         tr = rms([s['t'] for s in samples])
