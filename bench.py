@@ -25,7 +25,6 @@ step.
 import argparse
 import ctypes
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -295,7 +294,6 @@ def roofline(itf, x, args, lib):
     larger than L2 (129 MB)."""
     import torch
     from transiflow_gb300.vector import _stream
-    from transiflow_gb300.solver import _struct_ptr
     n = itf.n
     nnz = itf.pattern.nnz
     prob = itf._problem()
