@@ -1,35 +1,50 @@
-"""Newton, pseudo-arclength continuation and theta-method time integration.
+"""Newton's method, pseudo-arclength continuation and theta-method time
+stepping over any backend that honours TransiFlow's interface contract
+(``rhs``, ``jacobian``, ``solve``, ``mass_matrix``, ``set_parameter``).
 
-These are the callers of the hot path.  They only talk to the backend through
-the TransiFlow interface contract (``rhs``, ``jacobian``, ``solve``,
-``mass_matrix``, ``set_parameter``) and reproduce the control flow and the
-scalar arithmetic of the reference drivers, so a branch computed through the
-``CUDA`` backend follows the same sequence of parameter values, step-size
-adaptations and convergence decisions as one computed by the reference:
+The public classes take the constructor keywords and offer the methods of
+the reference drivers (``transiflow/Continuation.py:47-482``,
+``transiflow/TimeIntegration.py:29-115``), so scripts written for those run
+here too.  The numerics are Keller's pseudo-arclength method as Seydel
+states it (predictor 2.2.3, tangent 2.2.4-2.2.7, corrector 2.2.8-2.2.13),
+with the reference's choices for what the method leaves open: a forward
+difference of step ``delta`` for F_mu, the weight ``zeta = 1/N`` of the
+state in the arclength norm, the Newton-count step-size rule of
+Seydel p. 188 and a secant approach onto the target.  Evaluating those
+formulas in the same order makes a branch computed here follow the same
+parameter values, step sizes and accept/reject decisions as the reference's
+driver on the same backend (checked bit for bit against the reference in the
+tests).
 
-  Continuation     transiflow/Continuation.py:47-482
-  TimeIntegration  transiflow/TimeIntegration.py:29-115
+The organisation is this module's own: a step is a loop over attempts, each
+attempt is a corrector run described by a :class:`CorrectorResult`, and a
+branch is a loop over steps that ends by landing on the target.
 
-Vectors may be NumPy arrays or :class:`transiflow_gb300.vector.DeviceVector`;
-both support ``x.size``, ``.dot``, ``.T.conj() @ y`` and scalar arithmetic.
+Beyond the reference:
 
-Beyond the reference: an optional ``predictor`` callable can propose the
-continuation predictor (the learned surrogate of
-:mod:`transiflow_gb300.surrogate` plugs in here); the secant predictor of the
-reference is used whenever it is absent or its corrector does not converge
-within ``learned_newton_iterations`` iterations, and every accepted point is
-judged by the same Newton corrector.  An
-optional ``log`` callable receives one dict per accepted point.
+* ``predictor``: a callable ``(interface, x0, mu0, dx, dmu, ds)`` returning a
+  proposed point ``(x, mu)`` or ``None``.  The learned surrogate of
+  :mod:`transiflow_gb300.surrogate` plugs in here.  A proposal gets a
+  corrector budget of ``learned_newton_iterations``; when the corrector does
+  not converge within it, the same step is redone from the secant predictor
+  with the full budget.  Every accepted point is judged by the same corrector.
+* ``step_size``: a callable ``(interface, ds, iterations, ds_min, ds_max)``
+  returning the next step size, replacing the Newton-count rule after
+  accepted steps (failed attempts always halve by that rule).
+* ``log``: a callable receiving one dict per accepted point.
+* ``stats``: counts of interface calls, points and predictor outcomes.
+
+Vectors may be NumPy arrays or :class:`transiflow_gb300.vector.DeviceVector`.
 """
 
 import math
 import time
 
-__all__ = ['Continuation', 'TimeIntegration', 'dot', 'norm']
+__all__ = ['Continuation', 'TimeIntegration', 'CorrectorResult', 'dot', 'norm']
 
 
 def dot(x, y):
-    """utils.dot, transiflow/utils.py:5-11."""
+    """Inner product that works for NumPy arrays and device vectors."""
     try:
         return x.T.conj() @ y
     except AttributeError:
@@ -37,298 +52,381 @@ def dot(x, y):
 
 
 def norm(x):
-    """utils.norm for vectors, transiflow/utils.py:13-21."""
+    """Euclidean norm, ``sqrt(|x . x|)``."""
     return math.sqrt(abs(dot(x, x)))
 
 
-class Continuation:
-    """Pseudo-arclength continuation with a Newton corrector.
+class CorrectorResult:
+    """Outcome of one corrector run.
 
-    Same constructor keywords and defaults as transiflow.Continuation
-    (Continuation.py:47-51).  Bifurcation detection needs eigenvalues, which
-    the GPU backend does not provide; ``detect_bifurcations`` and
-    ``switch_branches`` therefore raise NotImplementedError.
+    ``converged`` is False when the run used its whole iteration budget or
+    saw the residual grow; ``x``/``mu`` are then the starting point."""
+
+    __slots__ = ('converged', 'x', 'mu', 'iterations', 'fnorm')
+
+    def __init__(self, converged, x, mu, iterations, fnorm):
+        self.converged = converged
+        self.x = x
+        self.mu = mu
+        self.iterations = iterations
+        self.fnorm = fnorm
+
+
+class _Calls:
+    """Interface calls with counters."""
+
+    def __init__(self, interface, stats):
+        self.itf = interface
+        self.stats = stats
+
+    def rhs(self, x):
+        self.stats['rhs'] += 1
+        return self.itf.rhs(x)
+
+    def jacobian(self, x):
+        self.stats['jacobian'] += 1
+        return self.itf.jacobian(x)
+
+    def solve(self, jac, *args):
+        self.stats['solve'] += 1
+        return self.itf.solve(jac, *args)
+
+    def at(self, name, value):
+        self.itf.set_parameter(name, value)
+
+
+class Continuation:
+    """Pseudo-arclength continuation of the steady states of an interface.
+
+    Keywords as in ``transiflow.Continuation``: ``delta`` (finite-difference
+    step of F_mu), ``destination_tolerance`` (how close to the target the
+    branch must end), ``newton_tolerance``, ``maximum_newton_iterations``,
+    ``optimal_newton_iterations`` (the step-size rule aims at this many
+    corrector iterations), ``residual_check`` ('F': stop on ||F||, 'dx': stop
+    on ||dx||), ``bordered_solver`` (solve the extended system in one call of
+    ``interface.solve``) and ``verbose``.  Bifurcation detection and branch
+    switching are not provided.
     """
 
     def __init__(self, interface, delta=1.0, destination_tolerance=1e-4,
                  newton_tolerance=1e-4, maximum_newton_iterations=10,
                  optimal_newton_iterations=3, residual_check='F',
                  bordered_solver=False, verbose=False, predictor=None, log=None, quiet=False,
-                 learned_newton_iterations=4):
+                 learned_newton_iterations=4, step_size=None):
+        if residual_check not in ('F', 'dx'):
+            raise ValueError("residual_check must be 'F' or 'dx'")
         self.interface = interface
-        self.quiet = quiet
-        self.verbose = verbose
-        self.destination_tolerance = destination_tolerance
         self.delta = delta
-        self.zeta = None
+        self.destination_tolerance = destination_tolerance
+        self.newton_tolerance = newton_tolerance
         self.maximum_newton_iterations = maximum_newton_iterations
         self.optimal_newton_iterations = optimal_newton_iterations
-        self.newton_tolerance = newton_tolerance
-        self.newton_iterations = 0
         self.residual_check = residual_check
         self.bordered_solver = bordered_solver
+        self.verbose = verbose
+        self.quiet = quiet
         self.predictor = predictor
         self.learned_newton_iterations = learned_newton_iterations
+        self.step_size = step_size
         self.log = log
+        self.zeta = None
+        self.newton_iterations = 0
         self.stats = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'points': 0,
                       'failed_correctors': 0, 'learned_accepted': 0, 'learned_rejected': 0}
-        self._t0 = None
+        self._calls = _Calls(interface, self.stats)
+        self._clock = None
 
-    def _say(self, *args, **kwargs):
-        """The reference's progress messages; quiet=True drops them (threads
-        driving instances concurrently cannot redirect a shared stdout)."""
+    # -- output ------------------------------------------------------------------
+    def _note(self, text):
         if not self.quiet:
-            print(*args, **kwargs)
+            print(text, flush=True)
 
-    # -- counted interface calls ---------------------------------------------
-    def _rhs(self, x):
-        self.stats['rhs'] += 1
-        return self.interface.rhs(x)
-
-    def _jac(self, x):
-        self.stats['jacobian'] += 1
-        return self.interface.jacobian(x)
-
-    def _solve(self, jac, *args):
-        self.stats['solve'] += 1
-        return self.interface.solve(jac, *args)
-
-    # -- Newton (Continuation.py:67-114) --------------------------------------
+    # -- Newton's method at a fixed parameter -----------------------------------------
     def newton(self, x0, tol=1e-10):
+        """Newton's method for F(x) = 0 at the current parameters, from x0.
+        Stops when ||F|| (or ||dx|| with residual_check='dx') drops below tol
+        or after maximum_newton_iterations; returns the last iterate."""
+        c = self._calls
+        on_f = self.residual_check == 'F'
         x = x0
-        k = 0
-        for k in range(self.maximum_newton_iterations):
-            fval = self._rhs(x)
-            if self.residual_check == 'F' or self.verbose:
-                fnorm = norm(fval)
-            if self.residual_check == 'F' and fnorm < tol:
-                self._say('Newton converged in %d iterations with ||F||=%e' % (k, fnorm), flush=True)
+        it = 0
+        for it in range(self.maximum_newton_iterations):
+            f = c.rhs(x)
+            fn = norm(f) if (on_f or self.verbose) else None
+            if on_f and fn < tol:
+                self._note('newton: ||F|| = %e after %d iterations' % (fn, it))
                 break
-            jac = self._jac(x)
-            dx = self._solve(jac, -fval)
-            x = x + dx
-            if self.residual_check != 'F' or self.verbose:
-                dxnorm = norm(dx)
-            if self.residual_check != 'F' and dxnorm < tol:
-                self._say('Newton converged in %d iterations with ||dx||=%e' % (k, dxnorm), flush=True)
+            step = c.solve(c.jacobian(x), -f)
+            x = x + step
+            sn = norm(step) if (not on_f or self.verbose) else None
+            if not on_f and sn < tol:
+                self._note('newton: ||dx|| = %e after %d iterations' % (sn, it))
                 break
             if self.verbose:
-                self._say('Newton status at iteration %d: ||F||=%e, ||dx||=%e' % (k, fnorm, dxnorm), flush=True)
-        self.newton_iterations = k
+                self._note('newton: iteration %d, ||F|| = %e, ||dx|| = %e' % (it, fn, sn))
+        self.newton_iterations = it
         return x
 
-    # -- corrector (Continuation.py:116-195) ----------------------------------
-    def _newton_corrector(self, name, ds, x, x0, mu, mu0, maxit=None):
-        maxit = self.maximum_newton_iterations if maxit is None else maxit
-        self.newton_iterations = 0
-        fnorm = None
-        dxnorm = None
-        self._last_fnorm = None
-        for k in range(maxit):
-            self.interface.set_parameter(name, mu)
-            fval = self._rhs(x)
-            if self.residual_check == 'F' or self.verbose:
-                prev_norm = fnorm
-                fnorm = norm(fval)
-                self._last_fnorm = fnorm
-            if self.residual_check == 'F' and fnorm < self.newton_tolerance:
-                self._say('Newton corrector converged in %d iterations with ||F||=%e' % (k, fnorm), flush=True)
-                break
-            if self.residual_check == 'F' and prev_norm is not None and prev_norm < fnorm:
-                self.newton_iterations = maxit
-                break
-            diff = x - x0
-            rnp1 = self.zeta * diff.dot(diff) + (1 - self.zeta) * (mu - mu0) ** 2 - ds ** 2
-            self.interface.set_parameter(name, mu + self.delta)
-            dflval = (self._rhs(x) - fval) / self.delta
-            self.interface.set_parameter(name, mu)
-            jac = self._jac(x)
-            if self.bordered_solver:
-                dx, dmu = self._solve(jac, -fval, -rnp1, dflval, 2 * self.zeta * diff,
-                                      2 * (1 - self.zeta) * (mu - mu0))
-            else:
-                z1 = self._solve(jac, -fval)
-                z2 = self._solve(jac, dflval)
-                dmu = (-rnp1 - 2 * self.zeta * diff.dot(z1)) / (2 * (1 - self.zeta) * (mu - mu0)
-                                                                - 2 * self.zeta * diff.dot(z2))
-                dx = z1 - dmu * z2
+    # -- the extended (arclength) system -------------------------------------------------
+    def _arclength_residual(self, diff, mu, mu0, ds):
+        """r = zeta |x - x0|^2 + (1 - zeta) (mu - mu0)^2 - ds^2 (Seydel 2.2.8)."""
+        z = self.zeta
+        return z * diff.dot(diff) + (1 - z) * (mu - mu0) ** 2 - ds ** 2
+
+    def _newton_update(self, name, x, mu, x0, mu0, f, ds):
+        """One Newton update (dx, dmu) of the extended system at (x, mu)."""
+        c = self._calls
+        z = self.zeta
+        diff = x - x0
+        r = self._arclength_residual(diff, mu, mu0, ds)
+        # F_mu by a forward difference (left-hand side of 2.2.9)
+        c.at(name, mu + self.delta)
+        f_mu = (c.rhs(x) - f) / self.delta
+        c.at(name, mu)
+        jac = c.jacobian(x)
+        if self.bordered_solver:
+            return c.solve(jac, -f, -r, f_mu, 2 * z * diff, 2 * (1 - z) * (mu - mu0))
+        # two solves with F_x and the Schur complement in mu (2.2.12, 2.2.13)
+        y_f = c.solve(jac, -f)
+        y_mu = c.solve(jac, f_mu)
+        dmu = (-r - 2 * z * diff.dot(y_f)) / (2 * (1 - z) * (mu - mu0) - 2 * z * diff.dot(y_mu))
+        return y_f - dmu * y_mu, dmu
+
+    def correct(self, name, x, mu, x0, mu0, ds, budget=None):
+        """Run the corrector from the predicted point (x, mu) on the arclength
+        sphere of radius ds around (x0, mu0).  ``x`` is updated in place.
+
+        The run stops successfully when ||F|| < newton_tolerance (or ||dx||
+        with residual_check='dx'); it fails when the monitored norm grows from
+        one iteration to the next or when the budget (default
+        maximum_newton_iterations) is used up."""
+        budget = self.maximum_newton_iterations if budget is None else budget
+        c = self._calls
+        on_f = self.residual_check == 'F'
+        tol = self.newton_tolerance
+        updates = 0
+        fn = sn = None
+        grew = False
+        for it in range(budget):
+            c.at(name, mu)
+            f = c.rhs(x)
+            if on_f or self.verbose:
+                last_fn, fn = fn, norm(f)
+            if on_f:
+                if fn < tol:
+                    self._note('corrector: ||F|| = %e after %d iterations' % (fn, it))
+                    break
+                if last_fn is not None and last_fn < fn:
+                    grew = True
+                    break
+            dx, dmu = self._newton_update(name, x, mu, x0, mu0, f, ds)
             x += dx
             mu += dmu
-            self.newton_iterations += 1
-            if self.residual_check != 'F' or self.verbose:
-                prev_norm = dxnorm
-                dxnorm = norm(dx)
-            if self.residual_check != 'F' and dxnorm < self.newton_tolerance:
-                self._say('Newton corrector converged in %d iterations with ||dx||=%e' % (k, dxnorm), flush=True)
+            updates += 1
+            if not on_f or self.verbose:
+                last_sn, sn = sn, norm(dx)
+            if not on_f and sn < tol:
+                self._note('corrector: ||dx|| = %e after %d iterations' % (sn, it))
                 break
             if self.verbose:
-                self._say('Newton corrector status at iteration %d: ||F||=%e, ||dx||=%e' % (k, fnorm, dxnorm), flush=True)
-            if self.residual_check != 'F' and prev_norm is not None and prev_norm < dxnorm:
-                self.newton_iterations = maxit
+                self._note('corrector: iteration %d, ||F|| = %e, ||dx|| = %e' % (it, fn, sn))
+            if not on_f and last_sn is not None and last_sn < sn:
+                grew = True
                 break
-        if self.newton_iterations == maxit:
-            self._say('Newton did not converge. Adjusting step size and trying again', flush=True)
-            self.stats['failed_correctors'] += 1
-            return x0, mu0
-        self.interface.set_parameter(name, mu)
-        return x, mu
+        # a run that used its whole budget counts as not converged, even when
+        # its last update met the tolerance
+        if grew or updates == budget:
+            self.newton_iterations = budget
+            self._note('corrector: no convergence, the step will be retried with a smaller ds')
+            return CorrectorResult(False, x0, mu0, budget, fn)
+        self.newton_iterations = updates
+        c.at(name, mu)
+        return CorrectorResult(True, x, mu, updates, fn)
 
-    # -- step-size control (Continuation.py:197-209) --------------------------
-    def _adjust_step_size(self, ds, ds_min, ds_max):
-        factor = self.optimal_newton_iterations / max(self.newton_iterations, 1)
-        factor = min(max(factor, 0.5), 2.0)
-        ds *= factor
+    # -- step size ----------------------------------------------------------------------
+    def _rescaled(self, ds, iterations, ds_min, ds_max):
+        """Seydel's rule: scale ds by optimal/actual corrector iterations,
+        within [1/2, 2], and clamp |ds| to [ds_min, ds_max]."""
+        ratio = min(max(self.optimal_newton_iterations / max(iterations, 1), 0.5), 2.0)
+        ds *= ratio
         ds = math.copysign(min(max(abs(ds), ds_min), ds_max), ds)
         if self.verbose:
-            self._say('New stepsize: ds=%e, factor=%e' % (ds, factor), flush=True)
+            self._note('step size: ds = %e (x%e)' % (ds, ratio))
         return ds
 
-    # -- converge onto the target (Continuation.py:234-249) -------------------
-    def _converge(self, name, x, mu, dx, dmu, target, ds, ds_min, ds_max, maxit):
-        for _ in range(maxit):
-            if abs(target - mu) < self.destination_tolerance:
-                self.interface.set_parameter(name, target)
-                self._say("Convergence achieved onto target %s = %f" % (name, mu), flush=True)
-                break
-            ds = 1 / dmu * (target - mu)
-            x, mu, dx, dmu, ds = self._step(name, x, mu, dx, dmu, ds, ds_min, ds_max)
-        return x, mu
+    def _next_step_size(self, ds, ds_min, ds_max):
+        if self.step_size is not None:
+            return self.step_size(self.interface, ds, self.newton_iterations, ds_min, ds_max)
+        return self._rescaled(ds, self.newton_iterations, ds_min, ds_max)
 
-    # -- one predictor/corrector step (Continuation.py:251-288) ---------------
-    def _step(self, name, x, mu, dx, dmu, ds, ds_min, ds_max, use_predictor=False):
-        mu0 = mu
-        x0 = x
-        learned = None
-        if use_predictor and self.predictor is not None:
-            learned = self.predictor(self.interface, x0, mu0, dx, dmu, ds)
-        if learned is not None:
-            x, mu = learned
-        else:
-            mu = mu0 + ds * dmu
-            x = x0 + ds * dx
-        x, mu = self._newton_corrector(name, ds, x, x0, mu, mu0,
-                                       self.learned_newton_iterations if learned is not None else None)
-        if learned is not None:
-            if mu == mu0:
-                # The learned predictor failed: fall back to the secant predictor.
-                self.stats['learned_rejected'] += 1
-                return self._step(name, x0, mu0, dx, dmu, ds, ds_min, ds_max)
-            self.stats['learned_accepted'] += 1
-        if mu == mu0:
-            prev_ds = ds
-            ds = self._adjust_step_size(ds, ds_min, ds_max)
-            if prev_ds == ds:
-                raise Exception('Newton cannot achieve convergence')
-            return self._step(name, x0, mu0, dx, dmu, ds, ds_min, ds_max)
-        self._say("%s: %f" % (name, mu), flush=True)
+    # -- one step along the branch ------------------------------------------------------
+    def _attempt(self, name, x0, mu0, dx, dmu, ds, proposal):
+        if proposal is not None:
+            x, mu = proposal
+            return self.correct(name, x, mu, x0, mu0, ds, self.learned_newton_iterations)
+        return self.correct(name, x0 + ds * dx, mu0 + ds * dmu, x0, mu0, ds)
+
+    def _advance(self, name, x0, mu0, dx, dmu, ds, ds_min, ds_max, learned):
+        """Take one step from (x0, mu0) along the tangent (dx, dmu); retries
+        with a reduced step size until the corrector converges.  Returns the
+        new point, the secant tangent through it and the step size used."""
+        proposal = None
+        if learned and self.predictor is not None:
+            proposal = self.predictor(self.interface, x0, mu0, dx, dmu, ds)
+        while True:
+            res = self._attempt(name, x0, mu0, dx, dmu, ds, proposal)
+            # a corrected point must have moved in the parameter: the secant
+            # tangent below divides by that change
+            ok = res.converged and res.mu != mu0
+            if proposal is not None:
+                proposal = None
+                if ok:
+                    self.stats['learned_accepted'] += 1
+                else:
+                    # redo the same step from the secant predictor
+                    self.stats['learned_rejected'] += 1
+                    continue
+            if ok:
+                break
+            self.stats['failed_correctors'] += 1
+            smaller = self._rescaled(ds, self.newton_iterations, ds_min, ds_max)
+            if smaller == ds:
+                raise Exception('continuation stalled: the corrector does not converge at the minimum step size')
+            ds = smaller
+        x, mu = res.x, res.mu
+        self._note('%s: %f' % (name, mu))
         self.stats['points'] += 1
         if self.log is not None:
-            self.log({'mu': mu, 'fnorm': self._last_fnorm, 'newton_iterations': self.newton_iterations,
-                      'ds': ds, 'wall_s': time.perf_counter() - (self._t0 or time.perf_counter())})
-        dmu = mu - mu0
-        dx = x - x0
-        if abs(dmu) < 1e-12:
-            raise Exception('dmu too small')
-        dx /= ds
-        dmu /= ds
-        return x, mu, dx, dmu, ds
+            self.log({'mu': mu, 'fnorm': res.fnorm, 'newton_iterations': res.iterations, 'ds': ds,
+                      'wall_s': time.perf_counter() - (self._clock or time.perf_counter())})
+        # secant tangent through the two points, per unit arclength (2.2.4)
+        dmu_new = mu - mu0
+        dx_new = x - x0
+        if abs(dmu_new) < 1e-12:
+            raise Exception('continuation stalled: parameter change below 1e-12')
+        dx_new /= ds
+        dmu_new /= ds
+        return x, mu, dx_new, dmu_new, ds
 
-    # -- initial tangent (Continuation.py:330-350) ----------------------------
-    def _initial_tangent(self, x, name, mu):
-        self.interface.set_parameter(name, mu + self.delta)
-        dflval = self._rhs(x)
-        self.interface.set_parameter(name, mu)
-        fval = self._rhs(x)
-        dflval = (dflval - fval) / self.delta
-        jac = self._jac(x)
-        dx = self._solve(jac, -dflval)
+    def _land(self, name, x, mu, dx, dmu, target, ds, ds_min, ds_max, maxit):
+        """Secant steps onto mu = target once the branch has passed it."""
+        for _ in range(maxit):
+            if abs(target - mu) < self.destination_tolerance:
+                self._calls.at(name, target)
+                self._note('reached %s = %f' % (name, mu))
+                break
+            ds = 1 / dmu * (target - mu)
+            x, mu, dx, dmu, ds = self._advance(name, x, mu, dx, dmu, ds, ds_min, ds_max, False)
+        return x, mu
+
+    def _first_tangent(self, name, x, mu):
+        """Tangent at the starting point from F_x dx = -F_mu, dmu = 1,
+        normalised in the arclength norm (2.2.5-2.2.7)."""
+        c = self._calls
+        c.at(name, mu + self.delta)
+        f_up = c.rhs(x)
+        c.at(name, mu)
+        f = c.rhs(x)
+        f_mu = (f_up - f) / self.delta
+        dx = c.solve(c.jacobian(x), -f_mu)
         dmu = 1
-        nrm = math.sqrt(self.zeta * dx.dot(dx) + dmu ** 2)
-        dmu /= nrm
-        dx /= nrm
+        scale = math.sqrt(self.zeta * dx.dot(dx) + dmu ** 2)
+        dmu /= scale
+        dx /= scale
         return dx, dmu
 
-    def _return(self, x, mu, dx, dmu, ds, callback, return_step):
+    # -- a branch ----------------------------------------------------------------------
+    def continuation(self, x0, parameter_name, start, target, ds, ds_min=0.01, ds_max=1000,
+                     dx=None, dmu=None, maxit=1000, detect_bifurcations=False,
+                     switch_branches=False, return_step=False, callback=None):
+        """Follow the branch through (x0, start) in ``parameter_name`` until
+        it reaches ``target``; returns the final (x, mu), plus the last step
+        (dx*ds, dmu*ds) with return_step=True.  ``dx``/``dmu`` give the
+        initial direction (a step, as returned with return_step), otherwise
+        the tangent is computed; ``callback(interface, x, mu)`` is called
+        before every step and at the end."""
+        if detect_bifurcations or switch_branches:
+            raise NotImplementedError('bifurcation detection and branch switching are not provided')
+        self._clock = time.perf_counter()
+        name = parameter_name
+        x, mu = x0, start
+        self.zeta = 1 / x.size
+        if dx is None or dmu is None:
+            dx, dmu = self._first_tangent(name, x, mu)
+        else:
+            dx = dx / ds
+            dmu = dmu / ds
+        for j in range(maxit):
+            mu_prev = mu
+            if callback is not None:
+                callback(self.interface, x, mu)
+            x, mu, dx, dmu, ds = self._advance(name, x, mu, dx, dmu, ds, ds_min, ds_max, True)
+            if (mu_prev < target <= mu) or (mu_prev > target >= mu):
+                x, mu = self._land(name, x, mu, dx, dmu, target, ds, ds_min, ds_max, maxit - j)
+                break
+            ds = self._next_step_size(ds, ds_min, ds_max)
         if callback is not None:
             callback(self.interface, x, mu)
         if return_step:
             return x, mu, dx * ds, dmu * ds
         return x, mu
 
-    # -- main loop (Continuation.py:361-482) ----------------------------------
-    def continuation(self, x0, parameter_name, start, target, ds, ds_min=0.01, ds_max=1000,
-                     dx=None, dmu=None, maxit=1000, detect_bifurcations=False,
-                     switch_branches=False, return_step=False, callback=None):
-        if detect_bifurcations or switch_branches:
-            raise NotImplementedError('bifurcation detection needs an eigenvalue solver')
-        self._t0 = time.perf_counter()
-        x = x0
-        mu = start
-        self.zeta = 1 / x.size
-        if dx is None or dmu is None:
-            dx, dmu = self._initial_tangent(x, parameter_name, mu)
-        else:
-            dx /= ds
-            dmu /= ds
-        for j in range(maxit):
-            mu0 = mu
-            if callback is not None:
-                callback(self.interface, x, mu)
-            x, mu, dx, dmu, ds = self._step(parameter_name, x, mu, dx, dmu, ds, ds_min, ds_max,
-                                            use_predictor=True)
-            if (mu >= target and mu0 < target) or (mu <= target and mu0 > target):
-                x, mu = self._converge(parameter_name, x, mu, dx, dmu, target,
-                                       ds, ds_min, ds_max, maxit - j)
-                return self._return(x, mu, dx, dmu, ds, callback, return_step)
-            ds = self._adjust_step_size(ds, ds_min, ds_max)
-        return self._return(x, mu, dx, dmu, ds, callback, return_step)
-
 
 class TimeIntegration:
-    """Theta-method time integration (TimeIntegration.py:29-115)."""
+    """Implicit theta-method time stepping, each step solved by Newton's
+    method: M (x_n - x) / (theta dt) + F(x) + (1 - theta)/theta F(x_n) = 0,
+    with Jacobian J(x) - M / (theta dt).  Keywords as in
+    ``transiflow.TimeIntegration``."""
 
     def __init__(self, interface, theta=1.0, newton_tolerance=1e-10,
-                 maximum_newton_iterations=10, residual_check='F', verbose=False):
+                 maximum_newton_iterations=10, residual_check='F', verbose=False, quiet=False):
         self.interface = interface
-        self.verbose = verbose
         self.theta = theta
-        self.maximum_newton_iterations = maximum_newton_iterations
         self.newton_tolerance = newton_tolerance
+        self.maximum_newton_iterations = maximum_newton_iterations
         self.residual_check = residual_check
+        self.verbose = verbose
+        self.quiet = quiet
 
-    def _newton(self, x0, dt):
-        x = x0
-        b0 = self.interface.rhs(x0)
-        mass = self.interface.mass_matrix()
-        for k in range(self.maximum_newton_iterations):
-            fval = mass @ (x0 - x) + dt * self.theta * self.interface.rhs(x) + dt * (1 - self.theta) * b0
-            fval /= self.theta * dt
-            if self.residual_check == 'F' or self.verbose:
-                fnorm = norm(fval)
-            if self.residual_check == 'F' and fnorm < self.newton_tolerance:
-                print('Newton converged i %d iterations with ||F||=%e' % (k, fnorm), flush=True)
+    def _note(self, text):
+        if not self.quiet:
+            print(text, flush=True)
+
+    def _implicit_step(self, x_old, dt):
+        itf = self.interface
+        on_f = self.residual_check == 'F'
+        theta = self.theta
+        f_old = itf.rhs(x_old)
+        mass = itf.mass_matrix()
+        x = x_old
+        for it in range(self.maximum_newton_iterations):
+            g = mass @ (x_old - x) + dt * theta * itf.rhs(x) + dt * (1 - theta) * f_old
+            g /= theta * dt
+            gn = norm(g) if (on_f or self.verbose) else None
+            if on_f and gn < self.newton_tolerance:
+                self._note('time step: ||G|| = %e after %d Newton iterations' % (gn, it))
                 break
-            jac = self.interface.jacobian(x) - mass / (self.theta * dt)
-            dx = self.interface.solve(jac, -fval)
-            x = x + dx
-            if self.residual_check != 'F' or self.verbose:
-                dxnorm = norm(dx)
-            if self.residual_check != 'F' and dxnorm < self.newton_tolerance:
-                print('Newton converged in %d iterations with ||dx||=%e' % (k, dxnorm), flush=True)
+            step = itf.solve(itf.jacobian(x) - mass / (theta * dt), -g)
+            x = x + step
+            sn = norm(step) if (not on_f or self.verbose) else None
+            if not on_f and sn < self.newton_tolerance:
+                self._note('time step: ||dx|| = %e after %d Newton iterations' % (sn, it))
                 break
             if self.verbose:
-                print('Newton status at iteration %d: ||F||=%e, ||dx||=%e' % (k, fnorm, dxnorm), flush=True)
+                self._note('time step: iteration %d, ||G|| = %e, ||dx|| = %e' % (it, gn, sn))
         return x
 
     def integration(self, x0, dt, tmax, callback=None):
-        x = x0
-        t = 0
+        """Steps of size dt from t = 0 until t >= tmax; returns (x, t).
+        ``callback(interface, x, t)`` is called at the start and after every
+        step."""
+        x, t = x0, 0
         if callback:
             callback(self.interface, x, t)
         while t < tmax:
-            x = self._newton(x, dt)
+            x = self._implicit_step(x, dt)
             t += dt
-            print("t = %f" % t, flush=True)
+            self._note('t = %f' % t)
             if callback:
                 callback(self.interface, x, t)
         return x, t

@@ -5,7 +5,8 @@
 provides the methods the drivers call -- ``vector``, ``rhs``, ``jacobian``,
 ``mass_matrix``, ``solve`` (SciPy.py:37-49, 311-315), ``set_parameter`` /
 ``get_parameter`` (BaseInterface.py:94-116), ``save_state`` /
-``load_state`` (BaseInterface.py:118-215) and ``vector_from_array`` /
+``load_state`` (BaseInterface.py:118-215; inherited from the reference's
+``BaseInterface`` when that package is importable) and ``vector_from_array`` /
 ``array_from_vector`` -- so ``Continuation`` and ``TimeIntegration`` run on
 it unchanged.  States live on the GPU as :class:`DeviceVector`; the
 discretisation, the Jacobian and the solves run in libtfcuda kernels.
@@ -68,30 +69,93 @@ from .solver import Solver
 from .vector import DeviceVector, _stream
 
 
-class _NumpyEncoder(json.JSONEncoder):
-    def default(self, obj):
-        if isinstance(obj, np.integer):
-            return int(obj)
-        if isinstance(obj, np.floating):
-            return float(obj)
-        if isinstance(obj, (complex, np.complexfloating)):
-            return {'__complex__': True, 'real': obj.real, 'imag': obj.imag}
-        if isinstance(obj, np.ndarray):
-            return obj.tolist()
-        return json.JSONEncoder.default(self, obj)
+def _jsonable(obj):
+    """``default`` hook of json.dump for the parameter files: NumPy scalars
+    and arrays become plain numbers and lists, complex numbers the tagged
+    object ``{"__complex__": true, "real": .., "imag": ..}``."""
+    if isinstance(obj, (complex, np.complexfloating)):
+        return {'__complex__': True, 'real': obj.real, 'imag': obj.imag}
+    if isinstance(obj, np.ndarray):
+        return obj.tolist()
+    if isinstance(obj, np.generic):
+        return obj.item()
+    raise TypeError('%s is not JSON serialisable' % type(obj).__name__)
 
 
-def _decode(obj):
-    if '__complex__' in obj:
-        return complex(obj['real'], obj['imag'])
-    return obj
+def _unjson(obj):
+    return complex(obj['real'], obj['imag']) if obj.get('__complex__') else obj
 
 
-class Interface:
+class _Checkpointing:
+    """Parameter access and state checkpoints when the reference package is
+    not importable (with it, ``transiflow.interface.BaseInterface`` provides
+    them).  The files are the reference's: ``<name>.params`` holds the
+    parameter dictionary as JSON (complex values tagged), ``<name>.npy`` the
+    state (BaseInterface.py:118-215)."""
+
+    def set_parameter(self, name, value):
+        self.parameters[name] = value
+
+    def get_parameter(self, name, default=0):
+        return self.parameters[name] if name in self.parameters else default
+
+    def save_json(self, name, obj):
+        with open(name, 'w') as f:
+            json.dump(obj, f, default=_jsonable)
+
+    def load_json(self, name):
+        with open(name) as f:
+            return json.load(f, object_hook=_unjson)
+
+    def save_parameters(self, name):
+        path = name + '.params'
+        self.save_json(path, self.parameters)
+        print('Wrote parameters to', path, flush=True)
+
+    def load_parameters(self, name):
+        path = name + '.params'
+        before = dict(self.parameters)
+        self.parameters.update(self.load_json(path))
+        print('Read parameters from', path, flush=True)
+        for key in self.parameters:
+            if self.parameters[key] != before.get(key):
+                print("Updated '%s' from %s to %s" % (key, before.get(key), self.parameters[key]), flush=True)
+
+    def save_state(self, name, x):
+        self.save_parameters(name)
+        path = name if name.endswith('.npy') else name + '.npy'
+        np.save(path, self.array_from_vector(x))
+        print('Wrote state to', path, flush=True)
+
+    def load_state(self, name):
+        self.load_parameters(name)
+        path = name if name.endswith('.npy') else name + '.npy'
+        x = np.load(path)
+        print('Read state from', path, flush=True)
+        return x
+
+
+try:
+    # the reference's interface base class, when its package is importable
+    from transiflow.interface.BaseInterface import BaseInterface as _ContractBase
+except ImportError:
+    _ContractBase = None
+
+_Base = _ContractBase if _ContractBase is not None else _Checkpointing
+
+
+class Interface(_Base):
+    """The CUDA backend.  Subclasses ``transiflow.interface.BaseInterface``
+    when the reference package is importable (parameter access and
+    checkpoints then come from there), a stand-in with the same file format
+    otherwise."""
+
     def __init__(self, parameters, nx, ny, nz=1, dim=None, dof=None, x=None, y=None, z=None,
                  boundary_conditions=None, device=None):
         if not torch.cuda.is_available():
             raise _lib.CudaBackendError('the CUDA backend needs a GPU')
+        if _ContractBase is not None:
+            _ContractBase.__init__(self, parameters, nx, ny, nz, dim, dof, x, y, z, boundary_conditions)
         self.lib = _lib.load()
         self.device = torch.device(device or 'cuda')
         self.parameters = parameters
@@ -151,15 +215,6 @@ class Interface:
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}
 
-    # -- parameters (BaseInterface.py:94-116, Discretization.py:145-184) -------
-    def set_parameter(self, name, value):
-        if name in self.parameters and self.get_parameter(name) == value:
-            return
-        self.parameters[name] = value
-
-    def get_parameter(self, name, default=0):
-        return self.parameters.get(name, default) if name in self.parameters else default
-
     def _problem(self):
         return grid.make_problem(self.parameters, self.nx, self.ny, self.nz, self.dim, self.dof,
                                  self.x, self.y, self.z, self._metric.data_ptr(), self._stride,
@@ -192,8 +247,8 @@ class Interface:
 
     # -- discretisation ------------------------------------------------------
     def _key(self, state):
-        return (state.data.data_ptr(), state.data._version, json.dumps(self.parameters, sort_keys=True,
-                                                                     cls=_NumpyEncoder, default=str))
+        return (state.data.data_ptr(), state.data._version,
+                json.dumps(self.parameters, sort_keys=True, default=lambda o: repr(o)))
 
     def rhs(self, state):
         """F(state), Discretization.rhs (Discretization.py:367-390)."""
@@ -286,41 +341,10 @@ class Interface:
             return lam[order][:num], V[:, order][:, :num]
         return lam[order][:num]
 
-    # -- checkpointing (BaseInterface.py:118-215) ---------------------------------
-    def save_json(self, name, obj):
-        with open(name, 'w') as f:
-            json.dump(obj, f, cls=_NumpyEncoder)
-
-    def save_parameters(self, name):
-        self.save_json(name + '.params', self.parameters)
-        print('Wrote parameters to', name + '.params', flush=True)
-
-    def save_state(self, name, x):
-        self.save_parameters(name)
-        if not name.endswith('.npy'):
-            name += '.npy'
-        np.save(name, self.array_from_vector(x))
-        print('Wrote state to', name, flush=True)
-
-    def load_json(self, name):
-        with open(name, 'r') as f:
-            return json.load(f, object_hook=_decode)
-
-    def load_parameters(self, name):
-        old = self.parameters.copy()
-        self.parameters.update(self.load_json(name + '.params'))
-        print('Read parameters from', name + '.params', flush=True)
-        for k, v in self.parameters.items():
-            if v != old.get(k):
-                print("Updated '{}' from {} to {}".format(k, old.get(k), v), flush=True)
-
     def load_state(self, name):
-        self.load_parameters(name)
-        if not name.endswith('.npy'):
-            name += '.npy'
-        x = np.load(name)
-        print('Read state from', name, flush=True)
-        return self.vector_from_array(x)
+        """The checkpointed state as a device vector (the base class reads it
+        into host memory)."""
+        return self.vector_from_array(super().load_state(name))
 
 
 def create(parameters, nx, ny, nz=1, dim=None, dof=None, boundary_conditions=None, backend='CUDA'):

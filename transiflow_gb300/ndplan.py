@@ -167,21 +167,22 @@ def build_plan(nx, ny, nz, dof, rowptr, cols, leaf_cells=48, pressure_var=None, 
     orow, ocol = owner[rows], owner[cols]
     tgt = np.where(p.height[orow] < p.height[ocol], orow,
                    np.where(p.height[orow] > p.height[ocol], ocol, np.minimum(orow, ocol)))
-    # position of r and c inside the target front
+    # position of r and c inside the target front: one sorted table of
+    # (node, unknown) keys over every front's index list, searched for all
+    # entries at once
+    node_of = np.repeat(np.arange(p.nnodes, dtype=np.int64), p.f)
+    local_of = np.arange(len(p.idx), dtype=np.int64) - p.idx_off[node_of]
+    keys = node_of * N + p.idx
+    korder = np.argsort(keys, kind='stable')
+    skeys = keys[korder]
+    slocal = local_of[korder]
     pos_r = np.full(len(rows), -1, dtype=np.int64)
     pos_c = np.full(len(rows), -1, dtype=np.int64)
-    for t in range(p.nnodes):
-        sel = np.flatnonzero(tgt == t)
-        if not len(sel):
-            continue
-        fidx = p.idx[p.idx_off[t]:p.idx_off[t + 1]]
-        order = np.argsort(fidx)
-        sf = fidx[order]
-        for src, dst in ((rows, pos_r), (cols, pos_c)):
-            q = np.searchsorted(sf, src[sel])
-            q = np.minimum(q, len(sf) - 1)
-            hit = sf[q] == src[sel]
-            dst[sel[hit]] = order[q[hit]]
+    for src, dst in ((rows, pos_r), (cols, pos_c)):
+        want = tgt * N + src
+        q = np.minimum(np.searchsorted(skeys, want), len(skeys) - 1)
+        hit = skeys[q] == want
+        dst[hit] = slocal[q[hit]]
     keep = (pos_r >= 0) & (pos_c >= 0)
     # an entry whose row and column are both boundary unknowns of its front
     # cannot occur for true couplings; padding entries that land there are
