@@ -253,6 +253,15 @@ typedef struct tf_nd_plan {
     const int64_t *d_piv_off;   /* nnodes + 1: pivot storage offsets (own)    */
     const int32_t *d_rank;      /* 0/1: position among the parent's children  */
     int64_t front_elems;        /* total front elements                       */
+    /* FP32 factorisations: tree heights whose widest front has at least this
+     * many rows are factored in outer blocks of 256 columns, each followed by
+     * one rank-256 trailing update on the tensor cores (tcgen05, TF32
+     * products, FP32 sums); 0 keeps rank-32 FP32 updates everywhere.        */
+    int32_t tc_min_front;
+    /* products of those updates: 1 = one TF32 product per term, 3 (or any
+     * other value) = operands split into TF32 high parts and remainders,
+     * three products per term, close to FP32 accuracy                        */
+    int32_t tc_terms;
 } tf_nd_plan;
 
 /* Numeric factorisation of the (gauged) stencil-CSR values.  d_fronts holds
@@ -263,6 +272,15 @@ int tf_nd_factor_f64(const tf_nd_plan *plan, const double *d_vals, double *d_fro
                      int32_t *d_piv, int32_t *d_info, tf_stream_t stream);
 int tf_nd_factor_f32(const tf_nd_plan *plan, const double *d_vals, float *d_fronts,
                      int32_t *d_piv, int32_t *d_info, tf_stream_t stream);
+/* One rank-w tensor-core trailing update of every front of tree height
+ * `height`: F[r][j] -= L[r][k0:E] U[k0:E][j] for r, j >= E = min(k0 + 256,
+ * n_own), FP32 fronts, TF32 products (terms = 1, or 3 for split operands)
+ * with FP32 accumulation (the step the
+ * FP32 factorisation runs after each outer block; exposed for tests).
+ * Needs only d_n_own, d_f, d_front_off, level_ptr, max_f and nlevels of the
+ * plan.  No counterpart in the reference (SuperLU, SciPy.py:151).          */
+int tf_nd_tc_update_f32(const tf_nd_plan *plan, int height, int k0, int terms, float *d_fronts,
+                        int32_t *d_info, tf_stream_t stream);
 /* In-place solve of the factored system: d_x (length n, FP64) holds the
  * right-hand side on entry and the solution on exit.  The f32 variant works
  * in single precision on the FP64 vector.                                    */

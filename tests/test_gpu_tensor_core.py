@@ -1,0 +1,126 @@
+"""The tensor-core (tcgen05, TF32) trailing update of the FP32 multifrontal
+LU against an FP64 product of the same TF32-rounded operands, and the blocked
+FP32 factorisation that uses it as a GMRES preconditioner."""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _tf32(a):
+    """Round FP32 values to TF32 (10 mantissa bits), nearest with ties away
+    from zero, as cvt.rna.tf32.f32 does."""
+    b = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
+    r = ((b + np.uint32(0x1000)) & np.uint32(0xFFFFE000)).view(np.float32)
+    return r
+
+
+def _plan(n_own, f, dev):
+    """A one-height plan descriptor with the given fronts (only what the
+    tensor-core update reads)."""
+    from transiflow_gb300 import _lib
+    n_own = np.asarray(n_own, np.int32)
+    f = np.asarray(f, np.int32)
+    off = np.zeros(len(f) + 1, np.int64)
+    off[1:] = np.cumsum(f.astype(np.int64) ** 2)
+    keep = {'n_own': torch.as_tensor(n_own).to(dev), 'f': torch.as_tensor(f).to(dev),
+            'off': torch.as_tensor(off).to(dev), 'level_ptr': np.array([0, len(f)], np.int32),
+            'max_f': np.array([f.max()], np.int32), 'max_own': np.array([n_own.max()], np.int32)}
+    s = _lib.NdPlan()
+    s.n = int(n_own.sum())
+    s.nnodes = len(f)
+    s.nlevels = 1
+    s.level_ptr = keep['level_ptr'].ctypes.data
+    s.max_own = keep['max_own'].ctypes.data
+    s.max_f = keep['max_f'].ctypes.data
+    s.d_n_own = keep['n_own'].data_ptr()
+    s.d_f = keep['f'].data_ptr()
+    s.d_front_off = keep['off'].data_ptr()
+    s.front_elems = int(off[-1])
+    return s, keep, off
+
+
+@pytest.mark.parametrize('k0', [0, 256])
+@pytest.mark.parametrize('terms', [1, 3])
+def test_tensor_core_update_matches_fp64_product(built_lib, k0, terms):
+    lib = built_lib
+    dev = torch.device('cuda')
+    # fronts of different sizes: full and partial 256-column blocks, a
+    # trailing part that is not a multiple of the 128 x 256 tile, a front
+    # whose own part ends before this block (left unchanged)
+    n_own = [700, 300, 530, 200]
+    f = [1500, 700, 531, 900]
+    s, keep, off = _plan(n_own, f, dev)
+    rng = np.random.default_rng(7)
+    host = rng.standard_normal(int(off[-1])).astype(np.float32)
+    fronts = torch.as_tensor(host).to(dev)
+    info = torch.zeros(1, dtype=torch.int32, device=dev)
+    code = lib.tf_nd_tc_update_f32(ctypes.byref(s), 0, k0, terms, fronts.data_ptr(), info.data_ptr(), None)
+    assert code == 0
+    out = fronts.cpu().numpy()
+    assert int(info.item()) == 0
+    for t in range(len(f)):
+        F0 = host[off[t]:off[t + 1]].reshape(f[t], f[t])
+        F1 = out[off[t]:off[t + 1]].reshape(f[t], f[t])
+        E = min(k0 + 256, n_own[t])
+        if E <= k0:
+            assert np.array_equal(F0, F1)
+            continue
+        a, b = F0[E:, k0:E], F0[k0:E, E:]
+        A, B = _tf32(a).astype(np.float64), _tf32(b).astype(np.float64)
+        if terms == 1:
+            prod = A @ B
+        else:
+            # the split products: hi*hi + hi*lo + lo*hi of TF32 parts
+            Al = _tf32(a - _tf32(a)).astype(np.float64)
+            Bl = _tf32(b - _tf32(b)).astype(np.float64)
+            prod = A @ B + A @ Bl + Al @ B
+            # and close to the exact FP32-operand product
+            exact = a.astype(np.float64) @ b.astype(np.float64)
+            assert np.all(np.abs(prod - exact) <= 1e-6 * (np.abs(a).astype(np.float64) @ np.abs(b)) + 1e-30)
+        want = F0[E:, E:].astype(np.float64) - prod
+        bound = np.abs(A) @ np.abs(B)
+        err = np.abs(F1[E:, E:].astype(np.float64) - want)
+        assert np.all(err <= 4e-6 * bound + 2e-7 * np.abs(want) + 1e-30), (t, err.max())
+        # everything outside the trailing block is untouched
+        mask = np.ones_like(F0, dtype=bool)
+        mask[E:, E:] = False
+        assert np.array_equal(F0[mask], F1[mask])
+
+
+@pytest.mark.parametrize('shape,params', [((16, 16, 16), {'Reynolds Number': 300}),
+                                          ((256, 256, 1), {'Reynolds Number': 2000})])
+def test_blocked_fp32_factorisation_preconditions_gmres(shape, params):
+    """FP32 fronts factored in 256-column blocks with tensor-core updates:
+    FGMRES reaches the same FP64 solution, in at most a few more iterations
+    than with the rank-32 FP32 updates."""
+    from transiflow_gb300 import Interface
+    nx, ny, nz = shape
+    ys, its = [], []
+    for tc in (False, True):
+        p = dict(params)
+        p['CUDA'] = {'Factor Precision': 'fp32', 'Tolerance': 1e-12, 'Tensor Cores': tc,
+                     'Tensor Core Min Front': 512}
+        itf = Interface(p, nx, ny, nz)
+        rng = np.random.default_rng(3)
+        x = itf.vector_from_array(0.3 * rng.standard_normal(itf.n))
+        J = itf.jacobian(x)
+        b = itf.vector_from_array(rng.standard_normal(itf.n))
+        it0 = itf.solver.stats['gmres_iterations']
+        y = itf.solve(J, b)
+        its.append(itf.solver.stats['gmres_iterations'] - it0)
+        bg = b.numpy()
+        bg[itf.dim] = 0
+        r = (J @ y).numpy() - bg
+        r[itf.dim] = 0
+        assert np.linalg.norm(r) / np.linalg.norm(bg) < 1e-11
+        assert int(itf.solver.info.item()) == 0
+        assert max(itf.solver.plan.max_f) >= 512
+        ys.append(y.numpy())
+    assert np.linalg.norm(ys[1] - ys[0]) / np.linalg.norm(ys[0]) < 1e-9
+    # split-TF32 products keep the factors close to FP32 quality
+    assert its[1] <= its[0] + 2, its

@@ -23,7 +23,7 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 # the assembly TU keeps the reference's separate multiply/add rounding
 SOURCES = [('tf_assemble.cu', ['-fmad=false']), ('tf_sparse.cu', []), ('tf_nd.cu', []), ('tf_nd_panel_f32.cu', []),
            ('tf_nd_panel_f64.cu', []),
-           ('tf_nd_inv.cu', []), ('tf_nd_flow.cu', []),
+           ('tf_nd_inv.cu', []), ('tf_nd_tc.cu', []), ('tf_nd_flow.cu', []),
            ('tf_nd_sweep.cu', []), ('tf_surrogate.cu', [])]
 
 TF_MAX_BC_OPS = 24
@@ -94,7 +94,8 @@ class NdPlan(ctypes.Structure):
                 ('d_ea_off', ctypes.c_void_p), ('d_ea_map', ctypes.c_void_p),
                 ('nscat', ctypes.c_int64), ('d_scat_pos', ctypes.c_void_p), ('d_scat_src', ctypes.c_void_p),
                 ('scat_level_ptr', ctypes.c_void_p), ('d_piv_off', ctypes.c_void_p),
-                ('d_rank', ctypes.c_void_p), ('front_elems', ctypes.c_int64)]
+                ('d_rank', ctypes.c_void_p), ('front_elems', ctypes.c_int64), ('tc_min_front', ctypes.c_int32),
+                ('tc_terms', ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p
@@ -115,6 +116,7 @@ _SIGNATURES = {
     'tf_csr_compact_workspace_bytes': ([_I], ctypes.c_size_t),
     'tf_gauge_values': ([_I, _P, _P, _P, _I, _P, _P], _I),
     'tf_spmv_f64': ([_I, _P, _P, _P, _P, _P, _D, _D, _P], _I),
+    'tf_nd_tc_update_f32': ([_P, _I, _I, _I, _P, _P, _P], _I),
     'tf_spmv_f32': ([_I, _P, _P, _P, _P, _P, _D, _D, _P], _I),
     'tf_diag_axpy': ([_I, _D, _P, _P, _P, _P], _I),
     'tf_add_diagonal': ([_I, _P, _P, _P, _D, _P, _P], _I),

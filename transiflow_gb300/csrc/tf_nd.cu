@@ -68,20 +68,28 @@ __device__ __forceinline__ void lower_rows(const DevPlan &P, int node0, int k, T
         if (c < nb) row[c] = x[c];
 }
 
-// Block row to the right of the panel: X = L_pp^-1 F[k:k+nb, j], j >= k+nb
+// Block row to the right of the panel: X = L_pp^-1 F[k:k+nb, j] for the
+// columns j of the update region `mode` (UPD_ALL: [k+nb, f); UPD_COLS: the
+// outer block's columns [k+nb, E); UPD_ROWS: the columns [E, f) right of it)
 template <typename T>
-__device__ __forceinline__ void urow_cols(const DevPlan &P, int node0, int k, T *fronts) {
+__device__ __forceinline__ void urow_cols(const DevPlan &P, int node0, int k, int K0, int mode, T *fronts) {
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
     if (k >= n) return;
     const int nb = min(NB, n - k);
-    if (k + nb + blockIdx.x * TRSM_THREADS >= f) return;
+    int jlo = k + nb, jhi = f;
+    if (mode != UPD_ALL) {
+        const int E = min(K0 + KB, n);
+        if (mode == UPD_COLS) jhi = E;
+        else jlo = E;
+    }
+    if (jlo + blockIdx.x * TRSM_THREADS >= jhi) return;
     T *F = fronts + P.front_off[node];
     __shared__ T L[NB][NB + 1];
     for (int t = threadIdx.x; t < nb * nb; t += TRSM_THREADS) L[t / nb][t % nb] = F[(size_t)(k + t / nb) * f + k + t % nb];
     __syncthreads();
-    const int j = k + nb + blockIdx.x * TRSM_THREADS + threadIdx.x;
-    if (j >= f) return;
+    const int j = jlo + blockIdx.x * TRSM_THREADS + threadIdx.x;
+    if (j >= jhi) return;
     T x[NB];
 #pragma unroll
     for (int c = 0; c < NB; ++c)
@@ -101,33 +109,55 @@ __device__ __forceinline__ void urow_cols(const DevPlan &P, int node0, int k, T 
         if (c < nb) F[(size_t)(k + c) * f + j] = x[c];
 }
 
-// Both triangular solves of one panel step in one launch (grid.z = 0: the
-// boundary rows, 1: the block row); they are independent of each other.
+// Both triangular solves of one panel step in one launch (grid.z + zbase =
+// 0: the boundary rows, 1: the block row over the columns of `mode`); they
+// are independent of each other.
 template <typename T>
-__global__ void __launch_bounds__(TRSM_THREADS) trsm_kernel(DevPlan P, int node0, int k, T *fronts) {
-    if (blockIdx.z == 0) lower_rows(P, node0, k, fronts);
-    else urow_cols(P, node0, k, fronts);
+__global__ void __launch_bounds__(TRSM_THREADS) trsm_kernel(DevPlan P, int node0, int k, int K0, int mode, int zbase,
+                                                            T *fronts) {
+    if (blockIdx.z + zbase == 0) lower_rows(P, node0, k, fronts);
+    else urow_cols(P, node0, k, K0, mode, fronts);
 }
 
-// Trailing update F[r][j] -= sum_q F[r][k+q] F[k+q][j], r, j >= k+nb
+// Rows [rlo, rhi) and columns [clo, chi) of the trailing update of the
+// panel at column k (see UPD_*).
+struct Region {
+    int rlo, rhi, clo, chi;
+};
+__device__ __forceinline__ Region update_region(int mode, int k, int nb, int K0, int n, int f) {
+    Region g{k + nb, f, k + nb, f};
+    if (mode != UPD_ALL) {
+        const int E = min(K0 + KB, n);
+        if (mode == UPD_COLS) {
+            g.chi = E;
+        } else {
+            g.rhi = E;
+            g.clo = E;
+        }
+    }
+    return g;
+}
+
+// Trailing update F[r][j] -= sum_q F[r][k+q] F[k+q][j] over one region
 template <typename T>
-__global__ void __launch_bounds__(THREADS) gemm_kernel(DevPlan P, int node0, int k, T *fronts) {
+__global__ void __launch_bounds__(THREADS) gemm_kernel(DevPlan P, int node0, int k, int K0, int mode, T *fronts) {
     const int node = node0 + blockIdx.z;
     const int n = P.n_own[node], f = P.f[node];
     if (k >= n) return;
     const int nb = min(NB, n - k);
-    const int r0 = k + nb + blockIdx.y * TM, c0 = k + nb + blockIdx.x * TN;
-    if (r0 >= f || c0 >= f) return;
+    const Region g = update_region(mode, k, nb, K0, n, f);
+    const int r0 = g.rlo + blockIdx.y * TM, c0 = g.clo + blockIdx.x * TN;
+    if (r0 >= g.rhi || c0 >= g.chi) return;
     T *F = fronts + P.front_off[node];
     __shared__ T As[NB][TM + 1];   // As[q][r]
     __shared__ T Bs[NB][TN + 1];   // Bs[q][c]
     for (int t = threadIdx.x; t < NB * TM; t += THREADS) {
         const int q = t % NB, r = t / NB;
-        As[q][r] = (q < nb && r0 + r < f) ? F[(size_t)(r0 + r) * f + k + q] : T(0);
+        As[q][r] = (q < nb && r0 + r < g.rhi) ? F[(size_t)(r0 + r) * f + k + q] : T(0);
     }
     for (int t = threadIdx.x; t < NB * TN; t += THREADS) {
         const int q = t / TN, c = t % TN;
-        Bs[q][c] = (q < nb && c0 + c < f) ? F[(size_t)(k + q) * f + c0 + c] : T(0);
+        Bs[q][c] = (q < nb && c0 + c < g.chi) ? F[(size_t)(k + q) * f + c0 + c] : T(0);
     }
     __syncthreads();
     // warp w owns rows [16 (w / 2), +16) and columns [32 (w % 2), +32) of the
@@ -135,7 +165,7 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(DevPlan P, int node0, int
     // pipe is the bound, and the last tiles of a front are often partial)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wr = (warp >> 1) * 16, wc = (warp & 1) * 32;
-    if (r0 + wr >= f || c0 + wc >= f) return;
+    if (r0 + wr >= g.rhi || c0 + wc >= g.chi) return;
     const int tr = wr + (lane >> 3) * 4, tc = wc + (lane & 7) * 4;
     T acc[4][4] = {};
 #pragma unroll 8
@@ -151,11 +181,11 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(DevPlan P, int node0, int
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
         const int r = r0 + tr + u;
-        if (r >= f) continue;
+        if (r >= g.rhi) continue;
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
             const int c = c0 + tc + v;
-            if (c < f) F[(size_t)r * f + c] -= acc[u][v];
+            if (c < g.chi) F[(size_t)r * f + c] -= acc[u][v];
         }
     }
 }
@@ -166,23 +196,25 @@ __global__ void __launch_bounds__(THREADS) gemm_kernel(DevPlan P, int node0, int
 // the large fronts; the 64 x 64 kernel above covers small ones and FP64).
 constexpr int TB = 128;
 
-__global__ void __launch_bounds__(THREADS) gemm128_kernel(DevPlan P, int node0, int k, float *fronts) {
+__global__ void __launch_bounds__(THREADS) gemm128_kernel(DevPlan P, int node0, int k, int K0, int mode,
+                                                         float *fronts) {
     const int node = node0 + blockIdx.z;
     const int n = P.n_own[node], f = P.f[node];
     if (k >= n) return;
     const int nb = min(NB, n - k);
-    const int r0 = k + nb + blockIdx.y * TB, c0 = k + nb + blockIdx.x * TB;
-    if (r0 >= f || c0 >= f) return;
+    const Region g = update_region(mode, k, nb, K0, n, f);
+    const int r0 = g.rlo + blockIdx.y * TB, c0 = g.clo + blockIdx.x * TB;
+    if (r0 >= g.rhi || c0 >= g.chi) return;
     float *F = fronts + P.front_off[node];
     __shared__ float As[NB][TB + 4];   // As[q][r]
     __shared__ float Bs[NB][TB + 4];   // Bs[q][c]
     for (int t = threadIdx.x; t < NB * TB; t += THREADS) {
         const int q = t % NB, r = t / NB;
-        As[q][r] = (q < nb && r0 + r < f) ? F[(size_t)(r0 + r) * f + k + q] : 0.f;
+        As[q][r] = (q < nb && r0 + r < g.rhi) ? F[(size_t)(r0 + r) * f + k + q] : 0.f;
     }
     for (int t = threadIdx.x; t < NB * TB; t += THREADS) {
         const int q = t / TB, c = t % TB;
-        Bs[q][c] = (q < nb && c0 + c < f) ? F[(size_t)(k + q) * f + c0 + c] : 0.f;
+        Bs[q][c] = (q < nb && c0 + c < g.chi) ? F[(size_t)(k + q) * f + c0 + c] : 0.f;
     }
     __syncthreads();
     const int tr = (threadIdx.x / 16) * 8, tc = (threadIdx.x % 16) * 8;
@@ -200,12 +232,12 @@ __global__ void __launch_bounds__(THREADS) gemm128_kernel(DevPlan P, int node0, 
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
         const int r = r0 + tr + u;
-        if (r >= f) continue;
+        if (r >= g.rhi) continue;
         float *row = F + (size_t)r * f;
 #pragma unroll
         for (int v = 0; v < 8; ++v) {
             const int c = c0 + tc + v;
-            if (c < f) row[c] -= acc[u][v];
+            if (c < g.chi) row[c] -= acc[u][v];
         }
     }
 }
@@ -497,6 +529,23 @@ int ensure_smem(const void *kernel, size_t bytes) {
     return TF_OK;
 }
 
+// One SIMT trailing update over a region of at most rows x cols per front.
+template <typename T>
+static void update(const DevPlan &D, int node0, int cnt, int k, int K0, int mode, int rows, int cols, T *fronts,
+                   cudaStream_t s) {
+    if constexpr (sizeof(T) == 4) {
+        if (rows >= 2 * TB || cols >= 2 * TB) {
+            dim3 g((cols + TB - 1) / TB, (rows + TB - 1) / TB, cnt);
+            gemm128_kernel<<<g, THREADS, 0, s>>>(D, node0, k, K0, mode, (float *)fronts);
+            launched();
+            return;
+        }
+    }
+    dim3 g((cols + TN - 1) / TN, (rows + TM - 1) / TM, cnt);
+    gemm_kernel<T><<<g, THREADS, 0, s>>>(D, node0, k, K0, mode, fronts);
+    launched();
+}
+
 template <typename T>
 int factor(const tf_nd_plan *p, const double *vals, T *fronts, int32_t *piv, int32_t *info, cudaStream_t s,
            const std::function<int(int)> *after_level) {
@@ -521,26 +570,38 @@ int factor(const tf_nd_plan *p, const double *vals, T *fronts, int32_t *piv, int
         const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
         if (cnt <= 0) continue;
         const int mo = p->max_own[h], mf = p->max_f[h];
-        for (int k = 0; k < mo; k += NB) {
-            if ((e = panel<T>(D, node0, cnt, k, mo - k, nsm, fronts, piv, info, s))) return e;
-            const int rest = mf - k - 1;
-            if (mf > 0) {
-                dim3 gl((mf + TRSM_THREADS - 1) / TRSM_THREADS, cnt, 2);
-                trsm_kernel<T><<<gl, TRSM_THREADS, 0, s>>>(D, node0, k, fronts); launched();
-            }
-            if (rest > 0) {
-                if constexpr (sizeof(T) == 4) {
-                    if (rest >= 2 * TB) {
-                        const int tiles = (rest + TB - 1) / TB;
-                        gemm128_kernel<<<dim3(tiles, tiles, cnt), THREADS, 0, s>>>(D, node0, k, (float *)fronts);
-                        launched();
-                        continue;
-                    }
+        // FP32 heights whose widest front has at least tc_min_front rows:
+        // two-level blocking with the tensor-core update per outer block;
+        // otherwise one level of rank-32 updates over the whole trailing front
+        const bool two_level = sizeof(T) == 4 && p->tc_min_front > 0 && mf >= p->tc_min_front;
+        const int bw = two_level ? KB : mo;
+        const int mode = two_level ? UPD_COLS : UPD_ALL;
+        const dim3 gl((mf + TRSM_THREADS - 1) / TRSM_THREADS, cnt, 2);
+        for (int K0 = 0; K0 < mo; K0 += bw) {
+            // the panels of the block; with two levels they update only the
+            // block's own columns, so that the row swaps of later panels of
+            // the block move rows whose other columns are all still untouched
+            for (int k = K0; k < mo && k < K0 + bw; k += NB) {
+                if ((e = panel<T>(D, node0, cnt, k, mo - k, nsm, fronts, piv, info, s))) return e;
+                if (mf > 0) {
+                    trsm_kernel<T><<<gl, TRSM_THREADS, 0, s>>>(D, node0, k, K0, mode, 0, fronts); launched();
                 }
-                const int tiles = (rest + TM - 1) / TM;
-                dim3 gg(tiles, tiles, cnt);
-                gemm_kernel<T><<<gg, THREADS, 0, s>>>(D, node0, k, fronts); launched();
+                const int rest = mf - k - 1;
+                if (rest > 0) update<T>(D, node0, cnt, k, K0, mode, rest, two_level ? KB : rest, fronts, s);
             }
+            if (!two_level) continue;
+            // the block row right of the block, U[K0:E][E:f) = L_blk^-1 F[K0:E][E:f),
+            // panel by panel after all of the block's swaps, then the rank-w
+            // update of everything right of and below the block
+            for (int k = K0; k < mo && k < K0 + KB; k += NB) {
+                const dim3 gu((mf + TRSM_THREADS - 1) / TRSM_THREADS, cnt, 1);
+                trsm_kernel<T><<<gu, TRSM_THREADS, 0, s>>>(D, node0, k, K0, UPD_ROWS, 1, fronts); launched();
+                const int rest = mf - k - 1;
+                if (rest > 0) update<T>(D, node0, cnt, k, K0, UPD_ROWS, KB, rest, fronts, s);
+            }
+            if constexpr (sizeof(T) == 4)
+                if ((e = tc_update(D, node0, cnt, K0, mf, p->tc_terms == 1 ? 1 : 3, (float *)fronts, info, s)))
+                    return e;
         }
         for (int rank = 0; rank < 2; ++rank) {
             dim3 ge(64, cnt);

@@ -19,6 +19,16 @@ constexpr int NB = 32;       // panel width
 constexpr int TM = 64;       // gemm tile rows
 constexpr int TN = 64;       // gemm tile cols
 constexpr int THREADS = 256;
+// Outer block of the two-level FP32 factorisation: the 32-column panels of a
+// block update only the block's columns and rows, the rest of the front gets
+// one rank-KB update on the tensor cores per block (tf_nd_tc.cu).
+constexpr int KB = 256;
+// Region of a SIMT trailing update (gemm kernels in tf_nd.cu), for the panel
+// at column k inside the outer block starting at K0, E = min(K0 + KB, n):
+//   UPD_ALL   rows and columns [k + nb, f)       (one-level factorisation)
+//   UPD_COLS  rows [k + nb, f), columns [k + nb, E)
+//   UPD_ROWS  rows [k + nb, E), columns [E, f)
+enum { UPD_ALL = 0, UPD_COLS = 1, UPD_ROWS = 2 };
 
 struct DevPlan {
     const int32_t *n_own, *f, *parent, *idx, *ea_map, *rank;
@@ -108,6 +118,12 @@ int inv_levels(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int
 // height (rows x cols at most per front).
 template <typename T, bool FWD>
 void bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, const T *fronts, double *x, cudaStream_t s);
+
+// Rank-w tensor-core update F[r][j] -= L[r][K0:E] U[K0:E][j], r, j >= E, of
+// every front of one tree height (FP32 fronts, TF32 products -- one term, or
+// three for split operands -- with FP32 sums).
+int tc_update(const DevPlan &D, int node0, int cnt, int K0, int mf, int terms, float *fronts, int32_t *info,
+              cudaStream_t s);
 
 // Pivoted LU of the 32-column panel at column k of every front of one tree
 // height (node0 .. node0+cnt-1, at most `rows` panel rows), including the

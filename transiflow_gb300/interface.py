@@ -44,6 +44,13 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       fronts with at most this many 32x32 factor tiles per
                       sweep run as one task (default 48); target tiles per task
                       of the other fronts (default 24)
+  'Tensor Cores'      FP32 factors: tree heights whose widest front has at
+                      least 'Tensor Core Min Front' (default 1024) rows are
+                      factored in blocks of 256 columns whose trailing updates
+                      run on the tensor cores (tcgen05, FP32 sums) (default
+                      True); 'Tensor Core Precision' 'tf32x3' (default:
+                      operands split into TF32 high parts and remainders,
+                      three products, close to FP32) or 'tf32' (one product)
   'Leaf Cells'        grid cells of a box at which nested dissection stops
                       splitting (default 48)
   'CUDA Graphs'       replay the factorisation and solve launch sequences from
@@ -210,7 +217,10 @@ class Interface(_Base):
                              flow_fuse_tiles=int(opts.get('Dataflow Fuse Tiles', 48)),
                              flow_chunk_tiles=int(opts.get('Dataflow Chunk Tiles', 24)),
                              leaf_cells=int(opts.get('Leaf Cells', 48)),
-                             sweep=opts.get('Sweep Apply', False))
+                             sweep=opts.get('Sweep Apply', False),
+                             tc_min_front=(int(opts.get('Tensor Core Min Front', 1024))
+                                           if opts.get('Tensor Cores', True) else 0),
+                             tc_terms=1 if opts.get('Tensor Core Precision', 'tf32x3') == 'tf32' else 3)
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

@@ -216,7 +216,12 @@ class _Engine:
         info = solver.info
         f64 = precision == 'fp64'
         fac_fn = lib.tf_nd_factor_f64 if f64 else lib.tf_nd_factor_f32
-        sp = _struct_ptr(plan.struct)
+        # this engine's copy of the plan descriptor (plans are shared between
+        # interfaces of the same grid; the factorisation options are not)
+        self.struct = _lib.NdPlan.from_buffer_copy(plan.struct)
+        self.struct.tc_min_front = solver.tc_min_front if not f64 else 0
+        self.struct.tc_terms = solver.tc_terms
+        sp = _struct_ptr(self.struct)
         dev = solver.itf.device
         if solver.inverse:
             # invert the own blocks once per factorisation; apply with
@@ -317,8 +322,14 @@ class Solver:
 
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
                  reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True, flow=False,
-                 flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48, sweep=False):
+                 flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48, sweep=False, tc_min_front=1024,
+                 tc_terms=3):
         self.itf = interface
+        # FP32 factorisations: heights whose widest front has at least this
+        # many rows use blocked rank-256 tensor-core updates (0: never)
+        self.tc_min_front = int(tc_min_front)
+        # 1: plain TF32 products; 3: split operands, close to FP32 accuracy
+        self.tc_terms = int(tc_terms)
         # grid cells at which nested dissection stops splitting a box
         self.leaf_cells = leaf_cells
         self.inverse = inverse
