@@ -1,29 +1,48 @@
-"""Benchmark: seconds to reach the Reynolds-number target on one GB300.
+"""Benchmark: seconds to reach the Reynolds-number target on one GB300,
+learned predictor + mixed precision against the plain FP64 GPU backend.
 
-Workload (the plain-GPU configuration of the headline metric): 2D
-lid-driven cavity, nx = ny = 256 (196,608 unknowns), FP64 assembly,
-Newton at Re = 0 from the zero state, then pseudo-arclength continuation in
-the Reynolds number from 0 to 5000 with ds = 200 and ||F|| <= 1e-8 at every
-point; linear solves by FP64 GMRES to 1e-10 relative residual, preconditioned
-by the nested-dissection LU of the gauged Jacobian.  One step = one complete
-branch.  Synthetic: the branch starts from the zero state (no dataset).
+Workload: 3D lid-driven cavity 64x64x64 (dof 4, 1,048,576 unknowns, lid on
+top), Newton at Re = 0 from the zero state, then pseudo-arclength
+continuation in the Reynolds number from 0 to 2000 with ds = 100, every
+accepted point at ||F|| <= 1e-8.  Two arms on the same GPU:
 
-  value      seconds per branch, the initial state already on the device
-  e2e        the same through the public API with host buffers: the initial
-             state is copied from pinned host memory and the final state read
-             back inside the timed region
-  roofline   the dominant kernel, timed live with CUDA events
-  cpu_baseline  the CPU oracle (NumPy assembly + SuperLU) per call on this
-             host, scaled by the branch's call counts
+  learned+mixed  the learned continuation predictor (a 4-layer 3D CNN with 32
+                 channels, BF16 weights, FP32 accumulation), the secant
+                 predictor as fallback, FP32 multifrontal factors with
+                 tensor-core trailing updates as the preconditioner of FP64
+                 flexible GMRES to 1e-10 (the residual, the Newton update and
+                 the arclength scalars in FP64).  One step = one complete
+                 branch; `value` is the mean over the timed steps.
+  plain FP64     the secant predictor and FP64 factors; run once per bench
+                 invocation and reported beside the learned arm.
 
-``--impl reference`` times the reference algorithm's CPU implementation on
-this host (the oracle restatement: the reference package itself is not
-installable on the GPU machine) on the same workload, one bounded sample per
-step.
+The predictor is trained before the timed region on the points of plain
+continuations of 32^3 and 48^3 cavities (Re 0 -> 2500, one branch per seed
+3..6 and grid, the seed drawing the branch's step from [0.5, 1.5] x
+--train-ds), run with the mixed solver.  Inputs are synthetic (the zero
+start state; no dataset).  The frontal matrices (77 GB in FP32) are far
+larger than L2, so no flush is needed between steps.
+
+  value      seconds per learned+mixed branch, start state already on the GPU
+  e2e        the same steps through the public API: the start state copied
+             from pinned host memory and the final state read back inside the
+             timed region
+  roofline   the dominant kernel of the learned+mixed branch, timed live
+  cpu_baseline  the oracle's CPU rhs / jacobian (a restatement of the
+             reference's discretisation) on this host, sampled at 32^3 and
+             scaled by the cell count, times the plain branch's call counts;
+             the reference's SuperLU solve at 1,048,576 3D unknowns does not
+             finish on a CPU, so this is a lower bound
+
+``--impl reference`` times the reference algorithm's CPU implementation (the
+oracle restatement: the reference package cannot travel to the GPU machine)
+on the same workload, one bounded sample per step.  ``--workload ldc2d``
+times the plain FP64 2D 256^2 branch (Re 0 -> 5000, ds = 200) instead.
 """
 
 import argparse
 import ctypes
+import gc
 import json
 import os
 import statistics
@@ -31,8 +50,6 @@ import subprocess
 import sys
 import threading
 import time
-import io
-import contextlib
 
 import numpy as np
 
@@ -48,52 +65,83 @@ def parse():
     ap.add_argument('--steps', type=int, default=3)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    ap.add_argument('--nx', type=int, default=256)
-    ap.add_argument('--target', type=float, default=5000.0)
-    ap.add_argument('--ds', type=float, default=200.0)
-    ap.add_argument('--precision', default='fp64', choices=['fp64', 'fp32'])
-    ap.add_argument('--tol', type=float, default=1e-10)
+    ap.add_argument('--workload', default='ldc3d', choices=['ldc3d', 'ldc2d'],
+                    help='ldc3d: the headline learned+mixed vs plain FP64 comparison; ldc2d: the plain 2D branch')
+    ap.add_argument('--nx', type=int, default=None, help='cells per direction (64 for ldc3d, 256 for ldc2d)')
+    ap.add_argument('--target', type=float, default=None, help='Re at the branch end (2000 / 5000)')
+    ap.add_argument('--ds', type=float, default=None, help='initial arclength step (100 / 200)')
+    ap.add_argument('--tol', type=float, default=1e-10, help='FGMRES relative tolerance')
+    ap.add_argument('--precision', default='fp64', choices=['fp64', 'fp32'], help='ldc2d: factor precision')
+    ap.add_argument('--no-plain', action='store_true', help='ldc3d: skip the plain FP64 arm')
     ap.add_argument('--no-baseline', action='store_true')
-    ap.add_argument('--profile', default=None, choices=['factor', 'solve', 'assemble'],
+    ap.add_argument('--train-grids', default='32,48', help='training grid sizes (cubes)')
+    ap.add_argument('--train-seeds', default='3,4,5,6', help='one training branch per seed and grid')
+    ap.add_argument('--train-target', type=float, default=2500.0, help='Re at the end of the training branches')
+    ap.add_argument('--train-ds', type=float, default=60.0,
+                    help='training branches: step drawn from [0.5, 1.5] x this, also their largest step')
+    ap.add_argument('--train-steps', type=int, default=150, help='Adam steps per grid and round')
+    ap.add_argument('--train-rounds', type=int, default=4, help='rounds over the training grids')
+    ap.add_argument('--reuse-its', type=int, default=None, help="'Reuse Iterations' (default: the backend's)")
+    ap.add_argument('--reuse-drift', type=float, default=None, help="'Reuse Drift' (default: the backend's)")
+    ap.add_argument('--no-tc', action='store_true', help='FP32 factors without tensor-core updates')
+    ap.add_argument('--profile', default=None, choices=['factor', 'solve', 'assemble', 'tc'],
                     help='run only a few launches of one stage (for ncu captures)')
-    ap.add_argument('--nz', type=int, default=1, help='cells in z (1: the 2D grid)')
+    ap.add_argument('--nz', type=int, default=None, help='--profile: cells in z (1: the 2D grid)')
+    ap.add_argument('--re', type=float, default=1000.0, help='Reynolds number of the --profile state')
     ap.add_argument('--batched', type=int, default=0,
                     help='time this many random lid-driven cavities (nx from 32..192, Re from [100, 4000], '
                          'seed 2) solved concurrently and one after the other, then exit')
-    ap.add_argument('--re', type=float, default=1000.0, help='Reynolds number of the --profile state')
-    ap.add_argument('--apply', default='levels', choices=['flow', 'levels', 'sweep'],
-                    help='application of the inverted factors: one dataflow launch or one launch per tree height')
-    ap.add_argument('--flow-fuse', type=int, default=48, help='dataflow apply: most factor tiles of a warp-task front')
-    ap.add_argument('--flow-chunk', type=int, default=24, help='dataflow apply: target tiles per CTA task')
     ap.add_argument('--leaf-cells', type=int, default=48, help='grid cells at which nested dissection stops')
-    ap.add_argument('--reuse-its', type=int, default=None, help="'Reuse Iterations' (default: the backend's)")
-    ap.add_argument('--no-inverse', action='store_true', help="'Inverse Apply': False (substitution solves)")
-    ap.add_argument('--reuse-drift', type=float, default=None, help="'Reuse Drift' (default: the backend's)")
-    ap.add_argument('--learned', action='store_true',
-                    help='train the learned predictor on plain branches of the --train-grids, then time the '
-                         'branch at --nx/--nz plain (FP64 factors) and learned (FP32 factors), then exit')
-    ap.add_argument('--train-grids', default='32,48', help='--learned: training grid sizes (cubes when --nz > 1)')
-    ap.add_argument('--train-seeds', default='3,4,5,6', help='--learned: one training branch per seed and grid')
-    ap.add_argument('--train-target', type=float, default=2500.0, help='--learned: Re at the end of training branches')
-    ap.add_argument('--train-steps', type=int, default=100, help='--learned: Adam steps per grid and round')
-    ap.add_argument('--train-rounds', type=int, default=4, help='--learned: rounds over the training grids')
-    ap.add_argument('--sweep-heights', type=int, default=0,
-                    help='with --apply sweep: tree heights nearest the root in the cooperative launch (0: all)')
-    return ap.parse_args()
+    a = ap.parse_args()
+    three = a.workload == 'ldc3d'
+    a.nx = a.nx or (64 if three else 256)
+    a.target = a.target or (2000.0 if three else 5000.0)
+    a.ds = a.ds or (100.0 if three else 200.0)
+    if a.nz is None:
+        a.nz = a.nx if three else 1
+    return a
+
+
+# Factor reuse of the 3D workload (both arms): a 64^3 factorisation costs
+# seconds (FP32) to a minute (FP64) against milliseconds per GMRES
+# iteration, so a reused factorisation may take up to the restart length in
+# iterations and the Jacobian may drift further before a refactorisation.
+REUSE_3D = {'Reuse Iterations': 50, 'Reuse Drift': 0.2}
+
+
+def solver_options(args, precision):
+    o = {'Factor Precision': precision, 'Tolerance': args.tol, 'Leaf Cells': args.leaf_cells}
+    if args.workload == 'ldc3d':
+        o.update(REUSE_3D)
+    if args.reuse_its is not None:
+        o['Reuse Iterations'] = args.reuse_its
+    if args.reuse_drift is not None:
+        o['Reuse Drift'] = args.reuse_drift
+    if args.no_tc:
+        o['Tensor Cores'] = False
+    return o
 
 
 def config(args):
-    if args.nz > 1:
-        n = 4 * args.nx * args.nx * args.nz
-        grid = '3D lid-driven cavity %dx%dx%d, dof 4' % (args.nx, args.nx, args.nz)
-    else:
-        n = 3 * args.nx * args.nx
-        grid = '2D lid-driven cavity %dx%d, dof 3' % (args.nx, args.nx)
-    return {'workload': '%s (%d unknowns), Newton at Re=0 then continuation '
+    n3 = args.nx * args.nx * args.nz
+    if args.workload == 'ldc3d':
+        n = 4 * n3
+        return {'workload': '3D lid-driven cavity %dx%dx%d, dof 4 (%d unknowns), Newton at Re=0 then continuation '
+                            'Re 0->%g, ds=%g, ||F||<=1e-8; timed: learned predictor + FP32/tensor-core factors '
+                            'under FP64 FGMRES to %g; beside it once: secant predictor + FP64 factors'
+                            % (args.nx, args.nx, args.nz, n, args.target, args.ds, args.tol),
+                'nx': args.nx, 'ny': args.nx, 'nz': args.nz, 'dof': 4, 'unknowns': n, 'target_re': args.target,
+                'ds': args.ds, 'newton_tolerance': 1e-8,
+                'training': 'plain continuations at %s^3, Re 0->%g, seeds %s' % (args.train_grids, args.train_target,
+                                                                                args.train_seeds),
+                'l2': 'working set larger than L2 (77 GB of FP32 frontal matrices at 64^3)',
+                'parallelism': 'replicas (one instance per GPU)'}
+    n = 3 * n3
+    return {'workload': '2D lid-driven cavity %dx%d, dof 3 (%d unknowns), Newton at Re=0 then continuation '
                         'Re 0->%g, ds=%g, ||F||<=1e-8, FP64 GMRES to %g + ND-LU (%s factors)'
-                        % (grid, n, args.target, args.ds, args.tol, args.precision),
-            'nx': args.nx, 'ny': args.nx, 'nz': args.nz, 'dof': 4 if args.nz > 1 else 3, 'unknowns': n,
-            'target_re': args.target, 'ds': args.ds, 'newton_tolerance': 1e-8,
+                        % (args.nx, args.nx, n, args.target, args.ds, args.tol, args.precision),
+            'nx': args.nx, 'ny': args.nx, 'nz': 1, 'dof': 3, 'unknowns': n, 'target_re': args.target,
+            'ds': args.ds, 'newton_tolerance': 1e-8,
             'l2': 'working set larger than L2 (1.1 GB of frontal matrices at 256^2)',
             'parallelism': 'replicas (one instance per GPU)'}
 
@@ -152,104 +200,182 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# GPU arm
+# headline: learned + mixed against plain FP64 (3D lid-driven cavity)
 # ---------------------------------------------------------------------------
-def run_branch(itf, Continuation, x0, args):
-    cont = Continuation(itf, newton_tolerance=1e-8)
-    with contextlib.redirect_stdout(io.StringIO()):
-        itf.set_parameter('Reynolds Number', 0.0)
-        x = cont.newton(x0)
-        x, mu = cont.continuation(x, 'Reynolds Number', 0.0, args.target, args.ds)
+def _free():
+    import torch
+    gc.collect()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+
+def _branch(itf, x0, args, predictor=None, log=None):
+    from transiflow_gb300 import Continuation
+    cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=predictor, log=log)
+    itf.set_parameter('Reynolds Number', 0.0)
+    x = cont.newton(x0)
+    x, mu = cont.continuation(x, 'Reynolds Number', 0.0, args.target, args.ds)
     return x, mu, cont
 
 
-def gpu_arm(args, rank, world, local):
-    import torch
-    from transiflow_gb300 import Continuation, Interface, _lib, dist
-    torch.cuda.set_device(local)
-    lib = _lib.load()
-    tuning = {}
-    if args.reuse_its is not None:
-        tuning['Reuse Iterations'] = args.reuse_its
-    if args.reuse_drift is not None:
-        tuning['Reuse Drift'] = args.reuse_drift
-    if args.no_inverse:
-        tuning['Inverse Apply'] = False
-    params = {'CUDA': {**tuning, 'Factor Precision': args.precision, 'Tolerance': args.tol,
-                       'Dataflow Apply': args.apply == 'flow', 'Sweep Apply': (args.sweep_heights or True) if args.apply == 'sweep' else False,
-                       'Dataflow Fuse Tiles': args.flow_fuse,
-                       'Dataflow Chunk Tiles': args.flow_chunk, 'Leaf Cells': args.leaf_cells}}
-    itf = Interface(params, args.nx, args.nx, args.nz)
-    n = itf.n
-    stream = torch.cuda.current_stream()
-
-    # warm-up branches (the first one also builds the elimination plan)
-    for _ in range(args.warmup):
-        x, mu, cont = run_branch(itf, Continuation, itf.vector(), args)
-    calls = dict(cont.stats)
-    calls['factorizations'] = None
-    fac0 = itf.solver.stats['factorizations']
-    x, mu, cont = run_branch(itf, Continuation, itf.vector(), args)
-    calls['factorizations'] = itf.solver.stats['factorizations'] - fac0
-    calls['gmres_iterations_last'] = itf.solver.stats['gmres_iterations']
+def _polish(itf, x, mu):
+    """The branch end polished by Newton to ||F|| <= 1e-12 (outside any timed
+    region), as a host array."""
+    from transiflow_gb300 import Continuation
     itf.set_parameter('Reynolds Number', mu)
-    fnorm_end = itf.rhs(x).norm()
+    return itf.array_from_vector(Continuation(itf, quiet=True).newton(x, 1e-12))
 
-    # ---- value: device-resident start state ----
+
+def train_predictor(args):
+    """Plain continuations at the training grids (mixed solver), then the
+    learned predictor trained on all of their points."""
+    import torch
+    from transiflow_gb300 import Continuation, Interface
+    from transiflow_gb300.surrogate import Recorder, Surrogate
+    t0 = time.perf_counter()
+    groups = []
+    for n in [int(v) for v in args.train_grids.split(',')]:
+        for seed in [int(v) for v in args.train_seeds.split(',')]:
+            itf = Interface({'CUDA': solver_options(args, 'fp32')}, n, n, n)
+            rec = Recorder()
+            cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=rec.predictor, log=rec.log)
+            itf.set_parameter('Reynolds Number', 0.0)
+            x0 = cont.newton(itf.vector())
+            ds = args.train_ds * float(np.random.default_rng(seed).uniform(0.5, 1.5))
+            cont.continuation(x0, 'Reynolds Number', 0.0, args.train_target, ds, ds_max=1.5 * args.train_ds)
+            groups.append(((n, n, n), rec.samples))
+            del itf, cont, x0
+            _free()
+    branches_s = time.perf_counter() - t0
+    net = Surrogate(4)
+    net.fit_scales([smp for _, g in groups for smp in g])
+    t1 = time.perf_counter()
+    losses = []
+    for r in range(args.train_rounds):
+        for dims, g in groups:
+            if g:
+                losses.append(float(net.train(g, dims, steps=args.train_steps, lr=2e-3, batch=4, seed=r)[-1]))
+    torch.cuda.synchronize()
+    info = {'branches': len(groups), 'points': sum(len(g) for _, g in groups), 'branches_s': branches_s,
+            'train_s': time.perf_counter() - t1, 'adam_steps': args.train_rounds * args.train_steps * len(groups),
+            'final_loss': losses[-1] if losses else None, 'parameters': net.parameters()}
+    return net, info
+
+
+def plain_arm(args):
+    """The plain FP64 GPU backend on the same branch, once: secant
+    predictor, FP64 factors (after one warm-up factorisation that builds the
+    plan and the buffers)."""
+    import torch
+    from transiflow_gb300 import Interface
+    itf = Interface({'CUDA': solver_options(args, 'fp64')}, args.nx, args.nx, args.nz)
+    x0 = itf.vector()
+    itf.set_parameter('Reynolds Number', 0.0)
+    itf.solve(itf.jacobian(x0), itf.rhs(x0))
+    torch.cuda.synchronize()
+    s0 = dict(itf.solver.stats)
+    log = []
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record()
+    x, mu, cont = _branch(itf, itf.vector(), args, log=log.append)
+    ev[1].record()
+    torch.cuda.synchronize()
+    t = ev[0].elapsed_time(ev[1]) / 1000.0
+    s1 = itf.solver.stats
+    out = {'value': t, 'unit': 's', 'points': cont.stats['points'], 'rhs': cont.stats['rhs'],
+           'jacobian': cont.stats['jacobian'], 'solve': cont.stats['solve'],
+           'factorizations': s1['factorizations'] - s0['factorizations'],
+           'gmres_iterations': s1['gmres_iterations'] - s0['gmres_iterations'],
+           'max_fnorm': max(r['fnorm'] for r in log if r['fnorm'] is not None),
+           'mus': [r['mu'] for r in log], 'final_re': mu}
+    xe = _polish(itf, x, mu)
+    del itf, x, x0, cont
+    _free()
+    return out, xe
+
+
+def learned_arm(args, net, rank, local):
+    """W warm-up and K timed learned+mixed branches, each from the zero state
+    copied from pinned host memory, the final state read back."""
+    import torch
+    from transiflow_gb300 import Interface, _lib, dist
+    from transiflow_gb300.surrogate import LearnedPredictor
+    lib = _lib.load()
+    itf = Interface({'CUDA': solver_options(args, 'fp32')}, args.nx, args.nx, args.nz)
+    pred = LearnedPredictor(net)
+    n = itf.n
+    host0 = torch.zeros(n, dtype=torch.float64).pin_memory()
+    for _ in range(args.warmup):
+        x, mu, cont = _branch(itf, itf.vector_from_array(host0.numpy()), args, pred)
+        itf.array_from_vector(x)
+    stream = torch.cuda.current_stream()
     clocks = ClockSampler(local)
     clocks.start()
     dist.barrier()
     torch.cuda.synchronize()
     l0 = lib.tf_launch_count()
-    g0 = itf.solver.stats['graph_kernel_launches']
     s0 = dict(itf.solver.stats)
-    t_dev = []
+    t_dev, t_e2e, logs = [], [], []
     for _ in range(args.steps):
-        x0 = itf.vector()
+        log = []
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        x0 = itf.vector_from_array(host0.numpy())
         ev0.record(stream)
-        x, mu, _ = run_branch(itf, Continuation, x0, args)
+        x, mu, cont = _branch(itf, x0, args, pred, log=log.append)
         ev1.record(stream)
+        xh = itf.array_from_vector(x)
         torch.cuda.synchronize()
+        t_e2e.append(time.perf_counter() - w0)
         t_dev.append(ev0.elapsed_time(ev1) / 1000.0)
-    launches = lib.tf_launch_count() - l0 + itf.solver.stats['graph_kernel_launches'] - g0
-    s1 = itf.solver.stats
-    solver_stats = {k: (s1[k] - s0[k]) / args.steps for k in ('factorizations', 'solves', 'gmres_iterations',
-                                                               'reused', 'refactored_after_reuse')}
+        logs.append(log)
+    launches = lib.tf_launch_count() - l0 + itf.solver.stats['graph_kernel_launches'] - s0['graph_kernel_launches']
     dist.barrier()
     clk = clocks.stop()
-    t_step = dist.max_over_ranks(statistics.mean(t_dev))
+    s1 = itf.solver.stats
+    per = {k: (s1[k] - s0[k]) / args.steps for k in ('factorizations', 'solves', 'gmres_iterations', 'reused',
+                                                      'refactored_after_reuse')}
+    fn = [r['fnorm'] for log in logs for r in log if r['fnorm'] is not None]
+    out = {'t_dev': dist.max_over_ranks(statistics.mean(t_dev)), 't_e2e': dist.max_over_ranks(statistics.mean(t_e2e)),
+           'launches': int(launches), 'clocks': clk, 'max_fnorm': max(fn), 'final_re': mu,
+           'branch': {'points': cont.stats['points'], 'rhs': cont.stats['rhs'], 'jacobian': cont.stats['jacobian'],
+                      'solve': cont.stats['solve'], 'learned_accepted': cont.stats['learned_accepted'],
+                      'learned_rejected': cont.stats['learned_rejected'], 'per_step_solver': per,
+                      'mus': [r['mu'] for r in logs[-1]], 'step_s': t_dev}}
+    out['end_state'] = _polish(itf, x, mu)
+    return out, itf
 
-    # ---- e2e: host buffers through the public API ----
-    host0 = torch.zeros(n, dtype=torch.float64).pin_memory()
-    t_e2e = []
-    dist.barrier()
-    torch.cuda.synchronize()
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        x0 = itf.vector_from_array(host0.numpy())
-        x, mu, _ = run_branch(itf, Continuation, x0, args)
-        out = itf.array_from_vector(x)
-        torch.cuda.synchronize()
-        t_e2e.append(time.perf_counter() - t0)
-    e2e = dist.max_over_ranks(statistics.mean(t_e2e))
-    dist.barrier()
 
-    roof = roofline(itf, x, args, lib)
+def headline_arm(args, rank, world, local):
+    """The learned+mixed arm timed per step, the plain FP64 arm once, the
+    predictor trained first."""
+    import torch
+    from transiflow_gb300 import dist
+    torch.cuda.set_device(local)
+    net, training = train_predictor(args)
+    plain, xp = (None, None) if args.no_plain else plain_arm(args)
+    res, itf = learned_arm(args, net, rank, local)
+    t_step, e2e = res['t_dev'], res['t_e2e']
+    n = itf.n
+    roof = roofline_3d(itf, args)
+    xl = res.pop('end_state')
+    diff = float(np.linalg.norm(xl - xp) / np.linalg.norm(xp)) if xp is not None else None
+    max_fn = max(res['max_fnorm'], plain['max_fnorm'] if plain else 0.0)
+    ok = max_fn <= 1e-8 and (diff is None or diff <= 1e-8)
     result = {'metric': METRIC, 'value': t_step, 'unit': 's', 'n_gpus': world, 'steps': args.steps,
               'warmup': args.warmup, 'ms_per_step': t_step * 1000.0, 'higher_is_better': False,
-              'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64' if args.precision == 'fp64' else 'f64+f32',
+              'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64+f32 (split-TF32 tensor-core factor updates)',
               'data': 'synthetic (zero initial state; no dataset)', 'config': config(args),
               'e2e': {'value': e2e, 'unit': 's', 'h2d_bytes_per_step': 8 * n, 'd2h_bytes_per_step': 8 * n},
-              'roofline': roof, 'clocks': clk, 'gpu_launches': int(launches),
-              'branch': {'points': calls.get('points'), 'rhs': calls.get('rhs'), 'jacobian': calls.get('jacobian'),
-                         'solve': calls.get('solve'), 'factorizations': calls.get('factorizations'),
-                         'final_re': mu, 'final_fnorm': fnorm_end, 'per_step_solver': solver_stats,
-                         'newton_steps_per_s': (calls.get('jacobian') or 0) / t_step}}
+              'roofline': roof, 'clocks': res['clocks'], 'gpu_launches': res['launches'],
+              'status': 'ok' if ok else 'failed: ||F|| %.3e, end-point difference %s' % (max_fn, diff),
+              'plain_fp64': plain, 'speedup_vs_plain_fp64': (plain['value'] / t_step) if plain else None,
+              'end_point_rel_diff_vs_plain': diff, 'max_fnorm': max_fn,
+              'learned_mixed': res['branch'], 'training': training}
     if rank == 0 and not args.no_baseline:
-        result['cpu_baseline'] = cpu_baseline(args, calls)
+        result['cpu_baseline'] = cpu_baseline_3d(args, plain or res['branch'])
     return result
 
 
@@ -257,9 +383,138 @@ def _peaks():
     try:
         with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
             p = json.load(f)
-        return float(p['hbm_gbs']), 'measured'
+        return float(p['hbm_gbs']), float(p['bf16_tflops']), 'measured'
     except (OSError, KeyError, ValueError):
-        return 6800.0, 'fallback'
+        return 6800.0, 1900.0, 'fallback'
+
+
+def _timed(fn, count):
+    import torch
+    st = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for i in range(count):
+        fn(i)
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1000.0 / count
+
+
+def _bandwidth_kernels(itf, reps=4):
+    """Fused assembly and FP64 SpMV timed over `reps` rotating buffer sets
+    (each larger than half of L2 at 64^3 and 256^2, together larger than L2)."""
+    import torch
+    from transiflow_gb300 import _lib
+    from transiflow_gb300.vector import _stream
+    lib = _lib.load()
+    n, nnz = itf.n, itf.pattern.nnz
+    prob = itf._problem()
+    gen = torch.Generator(device=itf.device).manual_seed(1)
+    states = [0.1 * torch.randn(n, dtype=torch.float64, device=itf.device, generator=gen) for _ in range(reps)]
+    rhs = [torch.empty(n, dtype=torch.float64, device=itf.device) for _ in range(reps)]
+    jv = [torch.empty(nnz, dtype=torch.float64, device=itf.device) for _ in range(reps)]
+
+    def asm(i):
+        lib.tf_assemble(ctypes.byref(prob), states[i % reps].data_ptr(), rhs[i % reps].data_ptr(),
+                        jv[i % reps].data_ptr(), _stream())
+
+    _timed(asm, reps)
+    t_asm = _timed(asm, 20)
+    rp, cp = itf.pattern.rowptr, itf.pattern.cols
+
+    def spmv(i):
+        lib.tf_spmv_f64(n, rp.data_ptr(), cp.data_ptr(), jv[i % reps].data_ptr(), states[i % reps].data_ptr(),
+                        rhs[(i + 1) % reps].data_ptr(), 1.0, 0.0, _stream())
+
+    _timed(spmv, reps)
+    t_spmv = _timed(spmv, 20)
+    hbm = _peaks()[0]
+    b_asm = 16 * n + 8 * nnz
+    b_spmv = 12 * nnz + 4 * (n + 1) + 16 * n
+    return states[0], {
+        'tf_assemble (F + J, fused)': {'s_per_launch': t_asm, 'bytes': b_asm, 'GB/s': b_asm / t_asm / 1e9,
+                                       'frac_hbm': b_asm / t_asm / 1e9 / hbm},
+        'tf_spmv_f64': {'s_per_launch': t_spmv, 'bytes': b_spmv, 'GB/s': b_spmv / t_spmv / 1e9,
+                        'frac_hbm': b_spmv / t_spmv / 1e9 / hbm}}
+
+
+# DRAM bytes (read + write) of one launch of the roofline kernel from one ncu
+# capture (see profiles/), keyed by (workload, grid).
+ROOF_TRAFFIC = {}
+
+
+def roofline_3d(itf, args):
+    """Live CUDA-event timings at the bench grid.  The roofline kernel is the
+    tensor-core trailing update of the FP32 factorisation (tc_update_kernel):
+    one launch at k0 = 0 over the tree height with the widest fronts, timed
+    alone on the plan's own front buffer (which is scribbled on, so the
+    factorisation is dropped afterwards).  Beside it: the fused assembly, the
+    SpMV, one factorisation and one preconditioner application."""
+    import torch
+    from transiflow_gb300 import _lib
+    from transiflow_gb300.vector import DeviceVector
+    lib = _lib.load()
+    hbm, bf16, which = _peaks()
+    x, kernels = _bandwidth_kernels(itf)
+    solver = itf.solver
+    J = itf.jacobian(DeviceVector(x))
+    fac = solver.factorization(J)
+    torch.cuda.synchronize()
+    t_fac = []
+    for _ in range(2):
+        J.lu = None
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fac = solver.factorization(J)
+        e1.record()
+        torch.cuda.synchronize()
+        t_fac.append(e0.elapsed_time(e1) / 1000.0)
+    v = torch.ones(itf.n, dtype=torch.float64, device=itf.device)
+    t_app = _timed(lambda i: fac.apply(v), 5)
+    plan = solver.plan
+    kernels['tf_nd_factor_inv_f32 (one factorisation, graph)'] = {
+        's_per_call': min(t_fac), 'flops': plan.flops, 'TFLOP/s': plan.flops / min(t_fac) / 1e12}
+    kernels['tf_nd_solve_inv_f32 (one preconditioner application, graph)'] = {'s_per_call': t_app}
+    # the tensor-core update alone
+    p = plan.host
+    h = int(np.argmax(plan.max_f))
+    nodes = p.levels[h]
+    E = np.minimum(256, p.n_own[nodes]).astype(np.float64)
+    rest = p.f[nodes].astype(np.float64) - E
+    flops = float(np.sum(2.0 * E * rest * rest))
+    c_bytes = float(np.sum(8.0 * rest * rest))
+    eng = solver._engine('fp32')
+    fronts, _ = solver._fronts_raw('fp32')
+    sp = ctypes.cast(ctypes.pointer(eng.struct), ctypes.c_void_p)
+    st = torch.cuda.current_stream().cuda_stream
+
+    def tc(i):
+        _lib.check(lib.tf_nd_tc_update_f32(sp, h, 0, solver.tc_terms, fronts.data_ptr(), solver.info.data_ptr(),
+                                           ctypes.c_void_p(st)), 'tf_nd_tc_update_f32')
+
+    tc(0)
+    t_tc = _timed(tc, 5)
+    solver._owner.pop('fp32', None)       # the fronts no longer hold a factorisation
+    achieved = flops / t_tc / 1e12
+    peak = bf16 / 2.0
+    kernels['tc_update_kernel (alone)'] = {'s_per_launch': t_tc, 'flops': flops, 'TFLOP/s': achieved,
+                                           'front_rw_bytes': c_bytes, 'GB/s': c_bytes / t_tc / 1e9}
+    return {'bound': 'tensor',
+            'kernel': 'tc_update_kernel<%d>: tcgen05 rank-256 trailing update of the FP32 fronts, %dx%dx%d tree '
+                      'height %d (%d fronts), %.1f GFLOP per launch' % (solver.tc_terms, args.nx, args.nx, args.nz,
+                                                                       h, len(nodes), flops / 1e9),
+            'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s', 'frac': achieved / peak,
+            'peak_source': 'TF32 dense rate taken as half the measured BF16 dense rate (%s: MEASURED_PEAKS.json '
+                           'bf16_tflops %.1f); split-TF32 issues %d tensor products per algorithmic one'
+                           % (which, bf16, solver.tc_terms),
+            'traffic': ROOF_TRAFFIC.get(('ldc3d', args.nx, h)),
+            'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (profiles/)',
+            'algorithmic_flops': flops, 'hbm_peak_gbs': hbm, 'hbm_peak_source': '%s (MEASURED_PEAKS.json hbm_gbs)'
+                                                                                 % which,
+            'kernels': kernels}
 
 
 def fp64_peak():
@@ -285,52 +540,15 @@ def fp64_peak():
 
 # DRAM bytes (read + write) of one factorisation with the inversion of its own
 # blocks, summed over its launches in one ncu capture of
-# `bench.py --profile factor` on a GB300.
+# `bench.py --workload ldc2d --profile factor` on a GB300.
 FACTOR_TRAFFIC = {(256, 1, 'fp64'): 6.353e9}
 
 
-def roofline(itf, x, args, lib):
-    """Live CUDA-event timing of the dominant kernels over rotating buffers
-    larger than L2 (129 MB)."""
+def roofline_2d(itf, x, args):
+    """The 2D plain workload: the FP64 factorisation against this GPU's FP64
+    GEMM rate (its trailing updates run on the FP64 pipe)."""
     import torch
-    from transiflow_gb300.vector import _stream
-    n = itf.n
-    nnz = itf.pattern.nnz
-    prob = itf._problem()
-    reps = 8
-    # rotating states and Jacobian value buffers: reps x (8n + 8 nnz) > L2
-    states = [x.data.clone() for _ in range(reps)]
-    rhs = [torch.empty(n, dtype=torch.float64, device=itf.device) for _ in range(reps)]
-    jv = [torch.empty(nnz, dtype=torch.float64, device=itf.device) for _ in range(reps)]
-    st = torch.cuda.current_stream()
-
-    def timed(fn, count):
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        for i in range(count):
-            fn(i % reps)
-        e1.record(st)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / 1000.0 / count
-
-    def asm(i):
-        lib.tf_assemble(ctypes.byref(prob), states[i].data_ptr(), rhs[i].data_ptr(), jv[i].data_ptr(), _stream())
-
-    timed(asm, reps)
-    t_asm = timed(asm, 40)
-    bytes_asm = 16 * n + 8 * nnz          # read x + write F, write J values
-    rp, cp = itf.pattern.rowptr, itf.pattern.cols
-
-    def spmv(i):
-        lib.tf_spmv_f64(n, rp.data_ptr(), cp.data_ptr(), jv[i].data_ptr(), states[i].data_ptr(),
-                        rhs[i].data_ptr(), 1.0, 0.0, _stream())
-
-    timed(spmv, reps)
-    t_spmv = timed(spmv, 40)
-    bytes_spmv = 12 * nnz + 4 * (n + 1) + 16 * n
-    # factorisation and solve of the current Jacobian
+    _, kernels = _bandwidth_kernels(itf)
     J = itf.jacobian(itf.vector_from_array(x.numpy()))
     fac = itf.solver.factorization(J)
     torch.cuda.synchronize()
@@ -339,49 +557,104 @@ def roofline(itf, x, args, lib):
         J.lu = None
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(st)
+        e0.record()
         fac = itf.solver.factorization(J)
-        e1.record(st)
+        e1.record()
         torch.cuda.synchronize()
         f_time.append(e0.elapsed_time(e1) / 1000.0)
     t_fac = min(f_time)
-    v = torch.ones(n, dtype=torch.float64, device=itf.device)
-    t_sol = timed(lambda i: fac.apply(v), 10)
-    peak, which = _peaks()
+    v = torch.ones(itf.n, dtype=torch.float64, device=itf.device)
+    t_sol = _timed(lambda i: fac.apply(v), 10)
+    hbm, _, which = _peaks()
     flops = itf.solver.plan.flops
     f64 = fp64_peak()
-    kernels = {
-        'tf_assemble (F + J, fused)': {'s_per_launch': t_asm, 'bytes': bytes_asm,
-                                       'GB/s': bytes_asm / t_asm / 1e9, 'frac_hbm': bytes_asm / t_asm / 1e9 / peak},
-        'tf_spmv_f64': {'s_per_launch': t_spmv, 'bytes': bytes_spmv, 'GB/s': bytes_spmv / t_spmv / 1e9,
-                        'frac_hbm': bytes_spmv / t_spmv / 1e9 / peak},
-        'tf_nd_factor (%s)' % args.precision: {'s_per_call': t_fac, 'flops': flops,
-                                                'TFLOP/s': flops / t_fac / 1e12},
-        'tf_nd_solve (%s)' % args.precision: {'s_per_call': t_sol},
-    }
-    # The dominant work of a branch is the multifrontal factorisation, one
-    # CUDA-graph launch per Jacobian; its trailing-update GEMMs are FP64
-    # issue bound, so it is compared with this GPU's dense FP64 GEMM rate
-    # (cuBLAS DGEMM measured live; MEASURED_PEAKS.json has no FP64 figure).
+    kernels['tf_nd_factor (%s)' % args.precision] = {'s_per_call': t_fac, 'flops': flops,
+                                                      'TFLOP/s': flops / t_fac / 1e12}
+    kernels['tf_nd_solve (%s)' % args.precision] = {'s_per_call': t_sol}
     a = flops / t_fac / 1e12
-    return {'bound': 'tensor', 'kernel': 'tf_nd_factor_%s: multifrontal LU graph (%dx%d, %.2f GFLOP per launch)'
+    return {'bound': 'fp64-pipe', 'kernel': 'tf_nd_factor_%s: multifrontal LU graph (%dx%d, %.2f GFLOP per launch)'
             % (args.precision, args.nx, args.nx, flops / 1e9),
             'achieved': a, 'peak': f64 if args.precision == 'fp64' else None, 'unit': 'TFLOP/s',
             'frac': a / f64 if args.precision == 'fp64' else None,
-            'peak_source': 'FP64 dense GEMM of this GPU measured in this run (cuBLAS DGEMM 4096^3)',
+            'peak_source': 'FP64 dense GEMM of this GPU measured in this run (cuBLAS DGEMM 4096^3); the FP64 '
+                           'factorisation runs on the FP64 pipe, not the tensor cores',
             'traffic': FACTOR_TRAFFIC.get((args.nx, args.nz, args.precision)),
             'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum over the launches of one '
                               'factorisation (caches flushed per kernel: an upper bound)',
-            'algorithmic_flops': flops, 'hbm_peak_gbs': peak,
+            'algorithmic_flops': flops, 'hbm_peak_gbs': hbm,
             'hbm_peak_source': '%s (MEASURED_PEAKS.json hbm_gbs)' % which, 'kernels': kernels}
+
+
+# ---------------------------------------------------------------------------
+# the plain 2D workload
+# ---------------------------------------------------------------------------
+def plain2d_arm(args, rank, world, local):
+    import torch
+    from transiflow_gb300 import Interface, _lib, dist
+    torch.cuda.set_device(local)
+    lib = _lib.load()
+    itf = Interface({'CUDA': solver_options(args, args.precision)}, args.nx, args.nx, 1)
+    n = itf.n
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        x, mu, cont = _branch(itf, itf.vector(), args)
+    calls = dict(cont.stats)
+    fac0 = itf.solver.stats['factorizations']
+    x, mu, cont = _branch(itf, itf.vector(), args)
+    calls['factorizations'] = itf.solver.stats['factorizations'] - fac0
+    itf.set_parameter('Reynolds Number', mu)
+    fnorm_end = itf.rhs(x).norm()
+    host0 = torch.zeros(n, dtype=torch.float64).pin_memory()
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    l0 = lib.tf_launch_count()
+    s0 = dict(itf.solver.stats)
+    t_dev, t_e2e = [], []
+    for _ in range(args.steps):
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        x0 = itf.vector_from_array(host0.numpy())
+        ev0.record(stream)
+        x, mu, _ = _branch(itf, x0, args)
+        ev1.record(stream)
+        itf.array_from_vector(x)
+        torch.cuda.synchronize()
+        t_e2e.append(time.perf_counter() - w0)
+        t_dev.append(ev0.elapsed_time(ev1) / 1000.0)
+    launches = lib.tf_launch_count() - l0 + itf.solver.stats['graph_kernel_launches'] - s0['graph_kernel_launches']
+    s1 = itf.solver.stats
+    per = {k: (s1[k] - s0[k]) / args.steps for k in ('factorizations', 'solves', 'gmres_iterations', 'reused',
+                                                      'refactored_after_reuse')}
+    dist.barrier()
+    clk = clocks.stop()
+    t_step = dist.max_over_ranks(statistics.mean(t_dev))
+    e2e = dist.max_over_ranks(statistics.mean(t_e2e))
+    roof = roofline_2d(itf, x, args)
+    result = {'metric': METRIC, 'value': t_step, 'unit': 's', 'n_gpus': world, 'steps': args.steps,
+              'warmup': args.warmup, 'ms_per_step': t_step * 1000.0, 'higher_is_better': False,
+              'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64' if args.precision == 'fp64' else 'f64+f32',
+              'data': 'synthetic (zero initial state; no dataset)', 'config': config(args),
+              'e2e': {'value': e2e, 'unit': 's', 'h2d_bytes_per_step': 8 * n, 'd2h_bytes_per_step': 8 * n},
+              'roofline': roof, 'clocks': clk, 'gpu_launches': int(launches),
+              'branch': {'points': calls.get('points'), 'rhs': calls.get('rhs'), 'jacobian': calls.get('jacobian'),
+                         'solve': calls.get('solve'), 'factorizations': calls.get('factorizations'),
+                         'final_re': mu, 'final_fnorm': fnorm_end, 'per_step_solver': per,
+                         'newton_steps_per_s': (calls.get('jacobian') or 0) / t_step}}
+    if rank == 0 and not args.no_baseline:
+        result['cpu_baseline'] = cpu_baseline_2d(args, calls)
+    return result
 
 
 # ---------------------------------------------------------------------------
 # CPU oracle timings (the reference algorithm on this host's cores)
 # ---------------------------------------------------------------------------
-def oracle_sample(nx, seed=1):
+def oracle_sample(nx, nz=1, solve=True, seed=1):
     from oracle.solve import Interface as OracleInterface
-    itf = OracleInterface({'Reynolds Number': 1000}, nx, nx)
+    itf = OracleInterface({'Reynolds Number': 1000}, nx, nx, nz)
     s = 0.1 * np.random.default_rng(seed).standard_normal(itf.vector().size)
     t = {}
     t0 = time.perf_counter()
@@ -390,25 +663,17 @@ def oracle_sample(nx, seed=1):
     t0 = time.perf_counter()
     J = itf.jacobian(s)
     t['jacobian'] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    itf.solve(J, f)
-    t['factor_solve'] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    itf.solve(J, f)
-    t['solve'] = time.perf_counter() - t0
+    if solve:
+        t0 = time.perf_counter()
+        itf.solve(J, f)
+        t['factor_solve'] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        itf.solve(J, f)
+        t['solve'] = time.perf_counter() - t0
     return t
 
 
-# Call counts of the branch (2D LDC 256^2, Re 0 -> 5000, ds = 200,
-# newton_tolerance 1e-8) as run by the continuation driver; the GPU arm
-# recomputes them live and the reference arm uses these.
-# Interface calls of the 256^2 branch (Re 0 -> 5000, ds = 200, ||F|| <= 1e-8) as
-# the reference's Continuation makes them on an exact solver; the SciPy
-# interface factors every Jacobian once (the LU is cached on the matrix).
-BRANCH_CALLS_256 = {'rhs': 111, 'jacobian': 47, 'solve': 92, 'factorizations': 47}
-
-
-def extrapolate(t, calls):
+def extrapolate_2d(t, calls):
     """Seconds of the reference's SciPy path for these call counts: one
     SuperLU factorisation per Jacobian (SciPy.py:151, cached on the matrix)."""
     nfac = calls['jacobian']
@@ -416,38 +681,72 @@ def extrapolate(t, calls):
             + max(calls['solve'] - nfac, 0) * t['solve'])
 
 
-def cpu_baseline(args, calls):
+def cpu_baseline_2d(args, calls):
     t = oracle_sample(args.nx)
-    est = extrapolate(t, calls)
-    return {'value': est, 'unit': 's', 'cores': 1, 'kind': 'port',
-            'sample': 'oracle (vectorised NumPy restatement of Discretization + SciPy SuperLU, '
-                      'single-threaded splu) at %dx%d: 1 rhs %.2fs, 1 jacobian %.2fs, 1 factor+solve %.2fs, '
-                      '1 solve %.2fs, scaled by the branch call counts %s (one factorisation per jacobian)'
+    return {'value': extrapolate_2d(t, calls), 'unit': 's', 'cores': 1, 'kind': 'port',
+            'sample': 'oracle (vectorised NumPy restatement of Discretization + SciPy SuperLU, single-threaded '
+                      'splu) at %dx%d: 1 rhs %.2fs, 1 jacobian %.2fs, 1 factor+solve %.2fs, 1 solve %.2fs, scaled '
+                      'by the branch call counts %s (one factorisation per jacobian)'
                       % (args.nx, args.nx, t['rhs'], t['jacobian'], t['factor_solve'], t['solve'],
                          {k: calls[k] for k in ('rhs', 'jacobian', 'solve')}),
             'host_cpus': os.cpu_count()}
 
 
+# the oracle's rhs / jacobian scale with the cell count: they are sampled
+# on the 32^3 grid and scaled to the bench grid
+SAMPLE_3D = 32
+
+
+def extrapolate_3d(t, calls, args):
+    scale = args.nx * args.nx * args.nz / float(SAMPLE_3D ** 3)
+    return (calls['rhs'] * t['rhs'] + calls['jacobian'] * t['jacobian']) * scale
+
+
+def cpu_baseline_3d(args, calls):
+    t = oracle_sample(SAMPLE_3D, SAMPLE_3D, solve=False)
+    return {'value': extrapolate_3d(t, calls, args), 'unit': 's', 'cores': 1, 'kind': 'port',
+            'sample': 'oracle (vectorised NumPy restatement of Discretization) at %d^3: 1 rhs %.2fs, 1 jacobian '
+                      '%.2fs, scaled by the cell count to %dx%dx%d and by the plain branch call counts '
+                      '(rhs %d, jacobian %d); the solves are left out: SuperLU on 1,048,576 3D unknowns does not '
+                      'finish on a CPU, so this is a lower bound' % (SAMPLE_3D, t['rhs'], t['jacobian'], args.nx,
+                                                                    args.nx, args.nz, calls['rhs'], calls['jacobian']),
+            'host_cpus': os.cpu_count()}
+
+
+# Interface calls of the reference-equivalent branches: 2D 256^2 (Re 0 ->
+# 5000, ds = 200) as the reference's Continuation makes them on an exact
+# solver (the SciPy interface factors every Jacobian once), and the plain
+# 3D 64^3 branch (Re 0 -> 2000, ds = 100) as measured on the GPU.
+BRANCH_CALLS_256 = {'rhs': 111, 'jacobian': 47, 'solve': 92, 'factorizations': 47}
+BRANCH_CALLS_64 = {'rhs': 85, 'jacobian': 36, 'solve': 70}
+
+
 def reference_arm(args, rank):
     if rank != 0:
         return None
-    calls = dict(BRANCH_CALLS_256)
-    if args.nx != 256 or args.nz != 1:
-        return {'impl': 'reference', 'unavailable': 'branch call counts are known for the 256x256 branch only'}
+    three = args.workload == 'ldc3d'
+    if three:
+        calls = dict(BRANCH_CALLS_64)
+        if args.nx != 64 or args.nz != 64:
+            return {'impl': 'reference', 'unavailable': 'branch call counts are known for the 64^3 branch only'}
+        sample = lambda: extrapolate_3d(oracle_sample(SAMPLE_3D, SAMPLE_3D, solve=False), calls, args)
+        text = ('per step one rhs and one jacobian of the oracle at %d^3 on this host, scaled by the cell count to '
+                '64^3 and by the branch call counts %s; SuperLU solves at 1,048,576 3D unknowns do not finish on a '
+                'CPU and are left out, so the value is a lower bound' % (SAMPLE_3D, calls))
+    else:
+        calls = dict(BRANCH_CALLS_256)
+        if args.nx != 256:
+            return {'impl': 'reference', 'unavailable': 'branch call counts are known for the 256x256 branch only'}
+        sample = lambda: extrapolate_2d(oracle_sample(args.nx), calls)
+        text = ('per step one rhs, one jacobian, one SuperLU factor+solve and one solve of the oracle at %dx%d on '
+                'this host, scaled by the branch call counts %s' % (args.nx, args.nx, calls))
     for _ in range(args.warmup):
-        oracle_sample(args.nx)
-    vals = []
-    for _ in range(args.steps):
-        t = oracle_sample(args.nx)
-        vals.append(extrapolate(t, calls))
-    v = statistics.mean(vals)
-    return {'metric': METRIC, 'value': v, 'unit': 's', 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
-            'ms_per_step': v * 1000.0, 'higher_is_better': False, 'scaling': 'weak', 'vs_baseline': None,
-            'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference', 'config': config(args),
-            'cpu_baseline': {'value': v, 'unit': 's', 'cores': 1, 'kind': 'port',
-                             'sample': 'per step one rhs, one jacobian, one SuperLU factor+solve and one solve '
-                                       'of the oracle at %dx%d on this host, scaled by the branch call counts %s'
-                                       % (args.nx, args.nx, calls)},
+        sample()
+    v = statistics.mean([sample() for _ in range(args.steps)])
+    return {'metric': METRIC, 'value': v, 'unit': 's', 'n_gpus': args.gpus, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': v * 1000.0, 'higher_is_better': False, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference', 'config': config(args),
+            'cpu_baseline': {'value': v, 'unit': 's', 'cores': 1, 'kind': 'port', 'sample': text},
             'e2e': {'value': v, 'unit': 's', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
 
 
@@ -458,12 +757,9 @@ def profile_stage(args):
     each timed with CUDA events on the launching stream."""
     import torch
     from transiflow_gb300 import Interface
-    p = {'Reynolds Number': args.re, 'CUDA': {'Factor Precision': args.precision, 'CUDA Graphs': False,
-                                              'Dataflow Apply': args.apply == 'flow',
-                                              'Sweep Apply': ((args.sweep_heights or True)
-                                                              if args.apply == 'sweep' else False),
-                                              'Dataflow Fuse Tiles': args.flow_fuse,
-                                              'Dataflow Chunk Tiles': args.flow_chunk, 'Leaf Cells': args.leaf_cells}}
+    opts = solver_options(args, args.precision)
+    opts['CUDA Graphs'] = False
+    p = {'Reynolds Number': args.re, 'CUDA': opts}
     itf = Interface(p, args.nx, args.nx, args.nz)
     s = 0.1 * np.random.default_rng(1).standard_normal(itf.n)
     x = itf.vector_from_array(s)
@@ -474,6 +770,28 @@ def profile_stage(args):
     first = time.perf_counter() - t0
     st = torch.cuda.current_stream()
     times = []
+    if args.profile == 'tc':
+        # the tensor-core update alone on the widest height (scribbles on the
+        # fronts; nothing is solved afterwards)
+        from transiflow_gb300 import _lib
+        lib = _lib.load()
+        plan = itf.solver.plan
+        h = int(np.argmax(plan.max_f))
+        eng = itf.solver._engine(args.precision)
+        fronts, _ = itf.solver._fronts_raw(args.precision)
+        sp = ctypes.cast(ctypes.pointer(eng.struct), ctypes.c_void_p)
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            _lib.check(lib.tf_nd_tc_update_f32(sp, h, 0, itf.solver.tc_terms, fronts.data_ptr(),
+                                               itf.solver.info.data_ptr(), ctypes.c_void_p(st.cuda_stream)),
+                       'tf_nd_tc_update_f32')
+            e1.record(st)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1000.0)
+        print(json.dumps({'profile': 'tc', 'nx': args.nx, 'nz': args.nz, 'height': h, 's_per_call': times}))
+        return
     for _ in range(3):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -523,82 +841,6 @@ def batched(args):
                       'unknowns': int(sum(3 * s['nx'] ** 2 for s in specs))}))
 
 
-def learned(args):
-    """The learned + mixed configuration against plain FP64 on one GPU.
-    Training: one plain FP64 branch (Re 0 -> --train-target, ||F|| <= 1e-8)
-    per training grid and seed, the seed drawing the initial step from
-    [0.5, 1.5] x --ds; the learned predictor is trained on all their points
-    (Adam, --train-rounds rounds of --train-steps steps per grid).  Timed:
-    Newton at Re = 0 and the branch to --target at --nx/--nz, plain (secant
-    predictor, FP64 factors) and learned (learned predictor, FP32 factors),
-    each after a short warm-up branch on the same grid; every point at
-    ||F|| <= 1e-8, the end points compared after Newton polishing at the
-    target."""
-    import torch
-    from transiflow_gb300 import Continuation, Interface
-    from transiflow_gb300.surrogate import LearnedPredictor, Recorder, Surrogate
-    three_d = args.nz > 1
-
-    def make(n, precision):
-        return Interface({'CUDA': {'Factor Precision': precision, 'Tolerance': args.tol}},
-                         n, n, n if three_d else 1)
-
-    t0 = time.perf_counter()
-    groups = []
-    for n in [int(v) for v in args.train_grids.split(',')]:
-        for seed in [int(v) for v in args.train_seeds.split(',')]:
-            itf = make(n, 'fp64')
-            rec = Recorder()
-            cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=rec.predictor, log=rec.log)
-            itf.set_parameter('Reynolds Number', 0.0)
-            x0 = cont.newton(itf.vector())
-            ds = args.ds * float(np.random.default_rng(seed).uniform(0.5, 1.5))
-            cont.continuation(x0, 'Reynolds Number', 0.0, args.train_target, ds)
-            groups.append(((n, n, n if three_d else 1), rec.samples))
-    branches_s = time.perf_counter() - t0
-    net = Surrogate(4 if three_d else 3)
-    net.fit_scales([smp for _, g in groups for smp in g])
-    t1 = time.perf_counter()
-    for r in range(args.train_rounds):
-        for dims, g in groups:
-            if g:
-                net.train(g, dims, steps=args.train_steps, lr=2e-3, batch=4, seed=r)
-    torch.cuda.synchronize()
-    train_s = time.perf_counter() - t1
-
-    def branch(precision, predictor):
-        itf = make(args.nx, precision)
-        fn = []
-        cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=predictor,
-                            log=lambda rec: fn.append(rec['fnorm']))
-        itf.set_parameter('Reynolds Number', 0.0)
-        cont.continuation(cont.newton(itf.vector()), 'Reynolds Number', 0.0, min(args.target, 2 * args.ds),
-                          args.ds)                                  # warm-up: plans, graphs
-        itf.set_parameter('Reynolds Number', 0.0)
-        fn.clear()
-        cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=predictor,
-                            log=lambda rec: fn.append(rec['fnorm']))
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        x = cont.newton(itf.vector())
-        x, mu = cont.continuation(x, 'Reynolds Number', 0.0, args.target, args.ds)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t
-        itf.set_parameter('Reynolds Number', args.target)
-        xp = Continuation(itf, quiet=True).newton(x, 1e-12).numpy()
-        return wall, dict(cont.stats), max(f for f in fn if f is not None), xp
-
-    plain_s, plain_stats, plain_f, xa = branch('fp64', None)
-    learned_s, learned_stats, learned_f, xb = branch('fp32', LearnedPredictor(net))
-    print(json.dumps({'learned': True, 'nx': args.nx, 'nz': args.nz, 'target_re': args.target, 'ds': args.ds,
-                      'plain_fp64_s': plain_s, 'learned_mixed_s': learned_s, 'speedup': plain_s / learned_s,
-                      'plain_stats': plain_stats, 'learned_stats': learned_stats,
-                      'max_fnorm': max(plain_f, learned_f),
-                      'end_point_rel_diff': float(np.linalg.norm(xb - xa) / np.linalg.norm(xa)),
-                      'train_grids': args.train_grids, 'train_seeds': args.train_seeds,
-                      'train_samples': sum(len(g) for _, g in groups), 'train_branches_s': branches_s,
-                      'train_s': train_s, 'parameters': net.parameters()}))
-
 
 def main():
     args = parse()
@@ -608,16 +850,15 @@ def main():
     if args.batched:
         batched(args)
         return
-    if args.learned:
-        learned(args)
-        return
     from transiflow_gb300 import dist
     rank, world, local = dist.init_from_env()
     try:
         if args.impl == 'reference':
             res = reference_arm(args, rank)
+        elif args.workload == 'ldc3d':
+            res = headline_arm(args, rank, world, local)
         else:
-            res = gpu_arm(args, rank, world, local)
+            res = plain2d_arm(args, rank, world, local)
         if rank == 0 and res is not None:
             print(json.dumps(res), flush=True)
     finally:

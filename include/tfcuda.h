@@ -210,8 +210,11 @@ size_t tf_vec_mdot_workspace_bytes(int n, int k);
  * inside the library that every GPU loading it holds until exit; nothing is
  * allocated per call.  k must not exceed 64 (TF_ERR_SIZE otherwise).  The
  * first call on a device looks up the array's device address with that
- * device current; make that first call before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race.                */
+ * device current and keeps it for the life of the process; make that first
+ * call before any stream capture.  After cudaDeviceReset on a device the
+ * kept address is stale: a process that resets a device must not call this
+ * entry point on it again.  All calls share the array: calls that overlap on
+ * the GPU race.                                                             */
 int tf_vec_mdot_noalloc(int n, int k, const double *d_V, long long ldv, const double *d_w,
                         double *d_out, tf_stream_t stream);
 /* w[i] -= sum_j V[j*ldv+i] * h[j]  (h device, k <= 256)                     */

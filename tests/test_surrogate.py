@@ -311,3 +311,22 @@ def test_learned_continuation_reaches_the_same_branch_end(trained):
     xa = polish.newton(x, 1e-12).numpy()
     xb = polish.newton(trained['x_plain'], 1e-12).numpy()
     assert np.linalg.norm(xa - xb) <= 1e-8 * np.linalg.norm(xb)
+
+
+def test_surrogate_rejects_fields_its_kernels_cannot_read():
+    """The surrogate's kernels take raw device pointers: host tensors, other
+    dtypes, strided views and fields of another grid size are refused before
+    any launch (checked here without a GPU)."""
+    from transiflow_gb300.surrogate import check_field
+    n = 4 * 27
+    with pytest.raises(ValueError, match='GPU'):
+        check_field(torch.zeros(n, dtype=torch.float64), n)
+    with pytest.raises(ValueError, match='torch tensor'):
+        check_field(np.zeros(n), n)
+    if torch.cuda.is_available():
+        with pytest.raises(ValueError, match='float64'):
+            check_field(torch.zeros(n, dtype=torch.float32, device='cuda'), n)
+        with pytest.raises(ValueError, match='contiguous'):
+            check_field(torch.zeros(2 * n, dtype=torch.float64, device='cuda')[::2], n)
+        with pytest.raises(ValueError, match='values'):
+            check_field(torch.zeros(n + 1, dtype=torch.float64, device='cuda'), n)

@@ -6,6 +6,8 @@
 
 #include "tf_nd.cuh"
 
+#include <mutex>
+
 namespace tf {
 namespace nd {
 
@@ -481,6 +483,28 @@ static int launch_panel(const DevPlan &D, int node0, int cnt, int k, int rows, T
     const size_t sm = sizeof(T) * (size_t)((rows + CL - 1) / CL) * PSTRIDE;
     const int e = ensure_smem((const void *)panel_cluster_kernel<T, CL>, sm);
     if (e) return e;
+    if (CL > 8) {
+        // clusters of more than 8 CTAs are a per-kernel opt-in
+        static std::mutex mu;
+        std::lock_guard<std::mutex> lock(mu);
+        if (cudaFuncSetAttribute((const void *)panel_cluster_kernel<T, CL>,
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+            cudaGetLastError();
+            return TF_ERR_SIZE;
+        }
+        // a cluster this large needs that many free SMs in one GPC
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(CL);
+        cfg.blockDim = dim3(THREADS);
+        cfg.dynamicSmemBytes = sm;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, (const void *)panel_cluster_kernel<T, CL>, &cfg) !=
+                cudaSuccess ||
+            clusters < 1) {
+            cudaGetLastError();
+            return TF_ERR_SIZE;
+        }
+    }
     panel_cluster_kernel<T, CL><<<cnt * CL, THREADS, sm, s>>>(D, node0, k, fronts, piv, info);
     launched();
     return TF_OK;
@@ -537,14 +561,19 @@ int panel(const DevPlan &D, int node0, int cnt, int k, int rows, int nsm, T *fro
         }
         if (e != TF_ERR_SIZE) return e;
     }
-    // larger panels: rows staged in shared memory, spread over up to 8 CTAs
-    for (int cl = panel_cluster_size(cnt, rows, nsm, 8); cl <= 8; cl *= 2) {
+    // larger panels: rows staged in shared memory, spread over up to 8 CTAs,
+    // or 16 (a non-portable cluster size) for the tallest FP32 panels
+    for (int cl = panel_cluster_size(cnt, rows, nsm, 8); cl <= 16; cl *= 2) {
         int e = TF_ERR_SIZE;
         switch (cl) {
         case 1: e = launch_panel<T, 1>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
         case 2: e = launch_panel<T, 2>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
         case 4: e = launch_panel<T, 4>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
-        default: e = launch_panel<T, 8>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
+        case 8: e = launch_panel<T, 8>(D, node0, cnt, k, rows, fronts, piv, info, s); break;
+        default:
+            if constexpr (sizeof(T) == 4)
+                if (cnt * 16 <= nsm) e = launch_panel<T, 16>(D, node0, cnt, k, rows, fronts, piv, info, s);
+            break;
         }
         if (e != TF_ERR_SIZE) return e;
     }

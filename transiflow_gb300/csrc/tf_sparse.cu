@@ -413,7 +413,8 @@ double *g_noalloc_ptr[kMaxDevices] = {};
 // Device address of the scratch array for the current device.  The host
 // symbol g_mdot_noalloc_scratch is only a stand-in for the array, not a
 // device address, so the address is looked up once per device with that
-// device current and cached.
+// device current and cached for the life of the process (a cudaDeviceReset
+// of that device invalidates it; the header says so).
 static int noalloc_scratch(double **out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return TF_ERR_CUDA;

@@ -44,10 +44,27 @@ def _ptr(t):
 
 
 def _snapshot(v):
-    """A copy of a continuation vector as a tensor (DeviceVector or NumPy)."""
+    """A copy of a continuation vector as a tensor (DeviceVector or NumPy;
+    NumPy vectors stay in host memory until the surrogate moves them)."""
     if isinstance(v, DeviceVector):
         return v.data.clone()
     return torch.tensor(np.asarray(v, dtype=np.float64))
+
+
+def check_field(t, n, name='field'):
+    """Raises ValueError unless t is a contiguous FP64 CUDA tensor of n
+    values: the surrogate's kernels read and write raw device pointers, so a
+    host tensor or a field of another grid must never reach them."""
+    if not isinstance(t, torch.Tensor):
+        raise ValueError('%s must be a torch tensor, not %s' % (name, type(t).__name__))
+    if t.device.type != 'cuda':
+        raise ValueError('%s must be on the GPU (got %s)' % (name, t.device))
+    if t.dtype != torch.float64:
+        raise ValueError('%s must be float64 (got %s)' % (name, t.dtype))
+    if not t.is_contiguous():
+        raise ValueError('%s must be contiguous' % name)
+    if t.numel() != n:
+        raise ValueError('%s has %d values, the grid needs %d' % (name, t.numel(), n))
 
 
 class Recorder:
@@ -155,7 +172,20 @@ class Surrogate:
         return b
 
     # -- the kernels in order ------------------------------------------------------
+    def _on_device(self, sample):
+        """The sample's fields on this surrogate's GPU (samples recorded from
+        NumPy continuation vectors are host tensors)."""
+        if all(sample[k].device == self.device for k in ('x0', 't', 'x1')):
+            return sample
+        out = dict(sample)
+        for k in ('x0', 't', 'x1'):
+            out[k] = sample[k].to(self.device, dtype=torch.float64).contiguous()
+        return out
+
     def _pack(self, b, x, t, mu, ds):
+        n = b['ncell'] * self.dof
+        check_field(x, n, 'state')
+        check_field(t, n, 'tangent')
         sc = self.scales
         sx = (ctypes.c_float * self.dof)(*sc['sx'])
         st = (ctypes.c_float * self.dof)(*sc['st'])
@@ -164,6 +194,9 @@ class Surrogate:
                    'tf_sg_pack')
 
     def _target(self, b, sample):
+        n = b['ncell'] * self.dof
+        for k in ('x0', 't', 'x1'):
+            check_field(sample[k], n, 'sample ' + k)
         ds = sample['ds']
         inv = (ctypes.c_double * self.dof)(*[1.0 / (ds * ds * s) for s in self.scales['sd']])
         _lib.check(self.lib.tf_sg_target(b['ncell'], self.dof, _ptr(sample['x0']), _ptr(sample['t']),
@@ -237,6 +270,7 @@ class Surrogate:
         (mean over its batch), read back once at the end."""
         if not samples:
             raise ValueError('no training samples')
+        samples = [self._on_device(smp) for smp in samples]
         if self.scales is None:
             self.fit_scales(samples)
         b = self._buffers(dims)
@@ -258,6 +292,7 @@ class Surrogate:
         secant predictor's error level)."""
         if self.scales is None:
             raise RuntimeError('fit_scales() or train() sets the scales first')
+        samples = [self._on_device(smp) for smp in samples]
         b = self._buffers(dims)
         out = torch.zeros(len(samples), dtype=torch.float64, device=self.device)
         for k, sample in enumerate(samples):
