@@ -324,6 +324,19 @@ int tf_nd_solve_inv_f64(const tf_nd_plan *plan, const double *d_fronts, const in
                         double *d_x, double *d_scratch, tf_stream_t stream);
 int tf_nd_solve_inv_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,
                         double *d_x, double *d_scratch, tf_stream_t stream);
+/* BF16 storage of an FP32 factorisation for its applications: the factor
+ * entries an application reads (every own row; the own columns of the
+ * boundary rows) of the inverted FP32 fronts, rounded to BF16 into d_out,
+ * which has the fronts' layout (plan->front_elems 2-byte elements; entries
+ * an application does not read are left as they are).  Call after
+ * tf_nd_factor_inv_f32 / tf_nd_invert_f32.  tf_nd_solve_inv_bf16 applies
+ * them with FP32 products and sums (d_x, d_scratch as for
+ * tf_nd_solve_inv_f32), reading half the bytes of the FP32 application.
+ * No counterpart in the reference (SuperLU keeps FP64 factors,
+ * SciPy.py:151).                                                            */
+int tf_nd_factors_to_bf16(const tf_nd_plan *plan, const float *d_fronts, uint16_t *d_out, tf_stream_t stream);
+int tf_nd_solve_inv_bf16(const tf_nd_plan *plan, const uint16_t *d_fronts, const int32_t *d_piv,
+                         double *d_x, double *d_scratch, tf_stream_t stream);
 
 /* The same application as tf_nd_solve_inv_* in ONE persistent launch: both
  * sweeps run as a task list over the elimination tree, each task waiting

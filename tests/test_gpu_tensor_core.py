@@ -124,3 +124,36 @@ def test_blocked_fp32_factorisation_preconditions_gmres(shape, params):
     assert np.linalg.norm(ys[1] - ys[0]) / np.linalg.norm(ys[0]) < 1e-9
     # split-TF32 products keep the factors close to FP32 quality
     assert its[1] <= its[0] + 2, its
+
+
+@pytest.mark.parametrize('shape,params', [((16, 16, 16), {'Reynolds Number': 300}),
+                                          ((48, 48, 1), {'Reynolds Number': 2000})])
+def test_bf16_factor_storage_preconditions_gmres(shape, params):
+    """FP32 factors applied from their BF16 copy (FP32 products): FGMRES
+    still reaches the FP64 tolerance and the same solution as with the FP32
+    copy (in more iterations)."""
+    from transiflow_gb300 import Interface
+    nx, ny, nz = shape
+    ys, its = [], []
+    for storage in ('fp32', 'bf16'):
+        p = dict(params)
+        p['CUDA'] = {'Factor Precision': 'fp32', 'Tolerance': 1e-12, 'Factor Storage': storage}
+        itf = Interface(p, nx, ny, nz)
+        rng = np.random.default_rng(5)
+        x = itf.vector_from_array(0.3 * rng.standard_normal(itf.n))
+        J = itf.jacobian(x)
+        b = itf.vector_from_array(rng.standard_normal(itf.n))
+        it0 = itf.solver.stats['gmres_iterations']
+        y = itf.solve(J, b)
+        its.append(itf.solver.stats['gmres_iterations'] - it0)
+        bg = b.numpy()
+        bg[itf.dim] = 0
+        r = (J @ y).numpy() - bg
+        r[itf.dim] = 0
+        assert np.linalg.norm(r) / np.linalg.norm(bg) < 1e-11
+        ys.append(y.numpy())
+    assert np.linalg.norm(ys[1] - ys[0]) / np.linalg.norm(ys[0]) < 1e-9
+    # BF16 rounding of the (inverted) factors makes the preconditioner much
+    # weaker: measured 5 -> 41 iterations at 16^3, which is why FP32 storage
+    # is the default; the BF16 copy must still converge well inside one restart
+    assert its[1] < 50, its

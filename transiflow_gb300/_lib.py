@@ -141,6 +141,8 @@ _SIGNATURES = {
     'tf_nd_solve_inv_workspace_bytes': ([_P], ctypes.c_size_t),
     'tf_nd_solve_inv_f64': ([_P, _P, _P, _P, _P, _P], _I),
     'tf_nd_solve_inv_f32': ([_P, _P, _P, _P, _P, _P], _I),
+    'tf_nd_factors_to_bf16': ([_P, _P, _P, _P], _I),
+    'tf_nd_solve_inv_bf16': ([_P, _P, _P, _P, _P, _P], _I),
     'tf_nd_flow_workspace_bytes': ([_P, _I, _I], ctypes.c_size_t),
     'tf_nd_flow_prepare': ([_P, _P, ctypes.c_size_t, _I, _I, _I], _I),
     'tf_nd_solve_flow_f64': ([_P, _P, _P, _P, _P, _P], _I),

@@ -24,6 +24,8 @@
 
 #include "tf_nd.cuh"
 
+#include <cuda_bf16.h>
+
 #include <algorithm>
 #include <vector>
 
@@ -286,6 +288,20 @@ static int factor_invert(const tf_nd_plan *p, const double *vals, T *fronts, int
 // x's own rows are written only by the backward product, so no launch reads
 // rows another CTA of the same launch writes.
 // ---------------------------------------------------------------------------
+// Factors may be stored in a narrower type than the one the products run in:
+// BF16 storage (converted from the FP32 factorisation) is applied in FP32.
+template <typename S>
+struct Arith {
+    using type = S;
+};
+template <>
+struct Arith<__nv_bfloat16> {
+    using type = float;
+};
+__device__ __forceinline__ float widen(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ float widen(float v) { return v; }
+__device__ __forceinline__ double widen(double v) { return v; }
+
 constexpr int VT = 128;            // rows (one thread each) per CTA of the row kernel
 constexpr int VW = 8;              // rows (one warp each) per CTA of the warp kernel
 
@@ -293,9 +309,10 @@ constexpr int VW = 8;              // rows (one warp each) per CTA of the warp k
 // of s), then a shuffle sum: five FP64 adds per row against the row's
 // length / 32 products per lane, in exchange for spreading the large fronts
 // near the root over many SMs.
-template <typename T, bool FWD>
-__global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0, const T *fronts,
+template <typename S, bool FWD>
+__global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0, const S *fronts,
                                                             const int32_t *piv, double *x, double *packed) {
+    using T = typename Arith<S>::type;
     extern __shared__ double s_gather[];   // forward: s[0 .. rmax), then their indices in x
     pdl_trigger();
     const int node = node0 + blockIdx.y;
@@ -310,9 +327,9 @@ __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0
         // reads before waiting for the previous launch
         const int r = rfirst + (threadIdx.x >> 5), lane = threadIdx.x & 31;
         if (r < n) {
-            const T *row = fronts + P.front_off[node] + (size_t)r * f;
+            const S *row = fronts + P.front_off[node] + (size_t)r * f;
             const int c0 = FWD ? 0 : r, c1 = FWD ? r : n;
-            for (int c = c0 + lane * (128 / sizeof(T)); c < c1; c += 32 * (128 / sizeof(T))) prefetch_l2(row + c);
+            for (int c = c0 + lane * (128 / sizeof(S)); c < c1; c += 32 * (128 / sizeof(S))) prefetch_l2(row + c);
         }
     }
     // the positions in x of s (pivot order) do not depend on earlier launches
@@ -331,16 +348,16 @@ __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0
     const int lane = threadIdx.x & 31;
     const int r = rfirst + (threadIdx.x >> 5);
     if (r >= n) return;
-    const T *row = fronts + P.front_off[node] + (size_t)r * f;
+    const S *row = fronts + P.front_off[node] + (size_t)r * f;
     const int c0 = FWD ? 0 : r, c1 = FWD ? r : n;
     T s0 = T(0), s1 = T(0);
     int c = c0 + lane;
 #pragma unroll 4
     for (; c + 32 < c1; c += 64) {
-        s0 += row[c] * (T)sv[c];
-        s1 += row[c + 32] * (T)sv[c + 32];
+        s0 += (T)widen(row[c]) * (T)sv[c];
+        s1 += (T)widen(row[c + 32]) * (T)sv[c + 32];
     }
-    if (c < c1) s0 += row[c] * (T)sv[c];
+    if (c < c1) s0 += (T)widen(row[c]) * (T)sv[c];
     T s = s0 + s1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -472,17 +489,110 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node
     }
 }
 
+// The boundary products with BF16-stored factors, products and sums in FP32.
+// cp.async has no 2-byte form and rows start at any 2-byte alignment, so a
+// warp loads each 32 x 32 tile with plain loads (a 64-byte segment per row,
+// all 32 rows in flight), widens it to FP32 in shared memory and forms one
+// row's dot product per lane; the next tile's loads are issued before the
+// current tile's products.
+template <bool FWD>
+__global__ void __launch_bounds__(BV_THREADS) inv_bnd_bf16_kernel(DevPlan P, int node0, int ctiles,
+                                                                  const __nv_bfloat16 *fronts, double *x,
+                                                                  double *packed) {
+    __shared__ float tiles[BV_WARPS][TILE];
+    __shared__ float v[BV_TILES * SB];
+    pdl_trigger();
+    const int node = node0 + blockIdx.y;
+    const int n = P.n_own[node], f = P.f[node];
+    const int rlo = FWD ? n : 0, rhi = FWD ? f : n;
+    const int clo = FWD ? 0 : n, chi = FWD ? n : f;
+    const int ccols = ctiles * SB;
+    const int rbase = rlo + blockIdx.x * BV_ROWS;
+    const int cbase = clo + blockIdx.z * ccols;
+    if (rbase >= rhi || cbase >= chi) return;
+    const int cend = min(chi, cbase + ccols);
+    const __nv_bfloat16 *F = fronts + P.front_off[node];
+    const int32_t *g = P.idx + P.idx_off[node];
+    double *pk = packed + P.idx_off[node];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r0 = rbase + warp * SB;
+    float *buf = tiles[warp];
+    // the first tile of the factors in registers before the wait
+    float nxt[SB];
+    auto fetch = [&](int c0) {
+        const bool colok = c0 + lane < cend;
+#pragma unroll
+        for (int i = 0; i < SB; ++i) {
+            const int r = r0 + i;
+            nxt[i] = (colok && r < rhi) ? __bfloat162float(F[(size_t)r * f + c0 + lane]) : 0.f;
+        }
+    };
+    if (r0 < rhi) fetch(cbase);
+    constexpr int PER = BV_TILES * SB / BV_THREADS;
+    int32_t vi[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int c = threadIdx.x + q * BV_THREADS;
+        vi[q] = (c < ccols && cbase + c < cend) ? (FWD ? cbase + c : g[cbase + c]) : -1;
+    }
+    pdl_wait();
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int c = threadIdx.x + q * BV_THREADS;
+        if (c < ccols) v[c] = vi[q] >= 0 ? (float)(FWD ? pk[vi[q]] : x[vi[q]]) : 0.f;
+    }
+    __syncthreads();
+    if (r0 >= rhi) return;
+    float s = 0.f;
+    for (int c0 = cbase; c0 < cend; c0 += SB) {
+#pragma unroll
+        for (int i = 0; i < SB; ++i) buf[i * TSTRIDE + lane] = nxt[i];
+        __syncwarp();
+        if (c0 + SB < cend) fetch(c0 + SB);
+        s += tile_dot_n(buf, v + (c0 - cbase), lane, cend - c0);
+        __syncwarp();
+    }
+    if (r0 + lane < rhi) {
+        if (FWD) atomicAdd(x + g[r0 + lane], -(double)s);
+        else atomicAdd(pk + r0 + lane, -(double)s);
+    }
+}
+
+// The factor entries an application reads -- every own row, and the own
+// columns of the boundary rows -- converted from FP32 to BF16 (round to
+// nearest) into a buffer with the fronts' layout.
+__global__ void factors_to_bf16_kernel(DevPlan P, int node0, const float *fronts, __nv_bfloat16 *out) {
+    const int node = node0 + blockIdx.y;
+    const int n = P.n_own[node], f = P.f[node];
+    const float *F = fronts + P.front_off[node];
+    __nv_bfloat16 *O = out + P.front_off[node];
+    const int64_t own = (int64_t)n * f, total = own + (int64_t)(f - n) * n;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t e;
+        if (t < own) {
+            e = t;
+        } else {
+            const int64_t u = t - own;
+            e = (int64_t)(n + u / n) * f + u % n;
+        }
+        O[e] = __float2bfloat16_rn(F[e]);
+    }
+}
+
 // The products of one application are launched with programmatic stream
 // serialisation (pdl: every launch but the first of the sequence), so each
 // starts reading its factors while the one before it finishes.
 template <typename T, bool FWD>
 static int inv_apply(const DevPlan &D, int node0, int cnt, int mo, const T *fronts, const int32_t *piv, double *x,
                      double *packed, bool pdl, cudaStream_t s) {
-    cudaError_t ce;
+    cudaError_t ce = cudaSuccess;
     // FP32 shuffles are cheap, so single precision always takes a warp per row
-    if (sizeof(T) == 8 && mo <= VS && cnt >= 256) {
-        ce = launch_pdl(pdl, inv_apply_rows_kernel<T, FWD>, dim3(1, cnt), dim3(VT), 0, s, D, node0, fronts, piv, x,
-                        packed);
+    bool rows = false;
+    if constexpr (sizeof(T) == 8) rows = mo <= VS && cnt >= 256;
+    if (rows) {
+        if constexpr (sizeof(T) == 8)
+            ce = launch_pdl(pdl, inv_apply_rows_kernel<T, FWD>, dim3(1, cnt), dim3(VT), 0, s, D, node0, fronts, piv,
+                            x, packed);
     } else {
         const size_t sm = FWD ? (sizeof(double) + sizeof(int32_t)) * (size_t)mo : 0;
         if (sm > 48 * 1024) {
@@ -504,8 +614,13 @@ static int inv_bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, int
     const int wide = rb * cnt * ((cols + BV_TILES * SB - 1) / (BV_TILES * SB));
     const int ctiles = wide >= 4 * nsm ? BV_TILES : 1;
     dim3 grid(rb, cnt, (cols + ctiles * SB - 1) / (ctiles * SB));
-    const cudaError_t ce = launch_pdl(pdl, inv_bnd_kernel<T, FWD>, grid, dim3(BV_THREADS),
-                                      sizeof(T) * 2 * BV_WARPS * TILE, s, D, node0, ctiles, fronts, x, packed);
+    cudaError_t ce;
+    if constexpr (sizeof(T) == 2)
+        ce = launch_pdl(pdl, inv_bnd_bf16_kernel<FWD>, grid, dim3(BV_THREADS), 0, s, D, node0, ctiles, fronts, x,
+                        packed);
+    else
+        ce = launch_pdl(pdl, inv_bnd_kernel<T, FWD>, grid, dim3(BV_THREADS), sizeof(T) * 2 * BV_WARPS * TILE, s, D,
+                        node0, ctiles, fronts, x, packed);
     launched();
     return ce == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
@@ -547,6 +662,20 @@ template int inv_levels<float>(const tf_nd_plan *, const DevPlan &, const float 
                                int, bool, cudaStream_t);
 template int inv_levels<double>(const tf_nd_plan *, const DevPlan &, const double *, const int32_t *, double *,
                                 double *, int, bool, cudaStream_t);
+
+// BF16 copy of the factor entries an application reads, one launch per height
+static int factors_to_bf16(const tf_nd_plan *p, const float *fronts, __nv_bfloat16 *out, cudaStream_t s) {
+    const DevPlan D = dev_plan(p, p->d_rank);
+    for (int h = 0; h < p->nlevels; ++h) {
+        const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
+        if (cnt <= 0) continue;
+        const int64_t per = (int64_t)p->max_own[h] * p->max_f[h] * 2;
+        const int bx = (int)std::min<int64_t>(std::max<int64_t>((per + 255) / 256, 1), 4096);
+        factors_to_bf16_kernel<<<dim3(bx, cnt), 256, 0, s>>>(D, node0, fronts, out);
+        launched();
+    }
+    return cuda_status();
+}
 
 }  // namespace nd
 }  // namespace tf
@@ -617,6 +746,24 @@ extern "C" int tf_nd_solve_inv_f64(const tf_nd_plan *plan, const double *d_front
     if (!d_fronts || !d_piv || !d_x || !d_scratch) return TF_ERR_ARG;
     return nd::solve_inv<double>(plan, nd::dev_plan(plan, plan->d_rank), d_fronts, d_piv, d_x, d_scratch,
                                  (cudaStream_t)stream);
+}
+
+extern "C" int tf_nd_factors_to_bf16(const tf_nd_plan *plan, const float *d_fronts, uint16_t *d_out,
+                                     tf_stream_t stream) {
+    int e = nd::check_plan(plan);
+    if (e) return e;
+    if (!d_fronts || !d_out) return TF_ERR_ARG;
+    return nd::factors_to_bf16(plan, d_fronts, reinterpret_cast<__nv_bfloat16 *>(d_out), (cudaStream_t)stream);
+}
+
+extern "C" int tf_nd_solve_inv_bf16(const tf_nd_plan *plan, const uint16_t *d_fronts, const int32_t *d_piv,
+                                    double *d_x, double *d_scratch, tf_stream_t stream) {
+    int e = nd::check_plan(plan);
+    if (e) return e;
+    if (!d_fronts || !d_piv || !d_x || !d_scratch) return TF_ERR_ARG;
+    return nd::solve_inv<__nv_bfloat16>(plan, nd::dev_plan(plan, plan->d_rank),
+                                        reinterpret_cast<const __nv_bfloat16 *>(d_fronts), d_piv, d_x, d_scratch,
+                                        (cudaStream_t)stream);
 }
 
 extern "C" int tf_nd_solve_inv_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,

@@ -51,6 +51,10 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       True); 'Tensor Core Precision' 'tf32x3' (default:
                       operands split into TF32 high parts and remainders,
                       three products, close to FP32) or 'tf32' (one product)
+  'Factor Storage'    FP32 factors: 'fp32' (default) or 'bf16' -- after each
+                      factorisation the entries the preconditioner reads are
+                      rounded to a BF16 copy, and every application reads
+                      that copy (half the bytes) with FP32 products and sums
   'Leaf Cells'        grid cells of a box at which nested dissection stops
                       splitting (default 48)
   'CUDA Graphs'       replay the factorisation and solve launch sequences from
@@ -220,7 +224,8 @@ class Interface(_Base):
                              sweep=opts.get('Sweep Apply', False),
                              tc_min_front=(int(opts.get('Tensor Core Min Front', 1024))
                                            if opts.get('Tensor Cores', True) else 0),
-                             tc_terms=1 if opts.get('Tensor Core Precision', 'tf32x3') == 'tf32' else 3)
+                             tc_terms=1 if opts.get('Tensor Core Precision', 'tf32x3') == 'tf32' else 3,
+                             storage=opts.get('Factor Storage', 'fp32'))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

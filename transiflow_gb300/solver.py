@@ -223,6 +223,12 @@ class _Engine:
         self.struct.tc_terms = solver.tc_terms
         sp = _struct_ptr(self.struct)
         dev = solver.itf.device
+        # FP32 factors may be applied from a BF16 copy (half the bytes)
+        self.bf16 = None
+        if not f64 and solver.storage == 'bf16':
+            if not solver.inverse or solver.flow or solver.sweep:
+                raise ValueError("BF16 factor storage needs 'Inverse Apply' with the per-height application")
+            self.bf16 = torch.empty(plan.front_elems, dtype=torch.bfloat16, device=dev)
         if solver.inverse:
             # invert the own blocks once per factorisation; apply with
             # parallel triangular products instead of substitution chains
@@ -267,10 +273,18 @@ class _Engine:
             else:
                 sbytes = lib.tf_nd_solve_inv_workspace_bytes(sp)
                 self.scratch = torch.empty(max(1, sbytes // 8), dtype=torch.float64, device=dev)
+                if self.bf16 is not None:
+                    # the FP32 factors' BF16 copy, applied in FP32
 
-                def solve():
-                    _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(),
-                                      self.scratch.data_ptr(), _stream()), 'tf_nd_solve_inv')
+                    def solve():
+                        _lib.check(lib.tf_nd_solve_inv_bf16(sp, self.bf16.data_ptr(), piv.data_ptr(),
+                                                            self.vec.data_ptr(), self.scratch.data_ptr(), _stream()),
+                                   'tf_nd_solve_inv_bf16')
+                else:
+
+                    def solve():
+                        _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(),
+                                          self.scratch.data_ptr(), _stream()), 'tf_nd_solve_inv')
 
             # the inversion of each height overlaps the factorisation of the
             # heights above it on a second stream
@@ -281,6 +295,9 @@ class _Engine:
                 _lib.check(facinv_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
                                      info.data_ptr(), self.work.data_ptr(), wbytes, _stream(),
                                      ctypes.c_void_p(self.aux.cuda_stream)), 'tf_nd_factor_inv')
+                if self.bf16 is not None:
+                    _lib.check(lib.tf_nd_factors_to_bf16(sp, fronts.data_ptr(), self.bf16.data_ptr(), _stream()),
+                               'tf_nd_factors_to_bf16')
         else:
             self.flow = None
             self.sweep = None
@@ -323,13 +340,17 @@ class Solver:
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
                  reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True, flow=False,
                  flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48, sweep=False, tc_min_front=1024,
-                 tc_terms=3):
+                 tc_terms=3, storage='fp32'):
         self.itf = interface
         # FP32 factorisations: heights whose widest front has at least this
         # many rows use blocked rank-256 tensor-core updates (0: never)
         self.tc_min_front = int(tc_min_front)
         # 1: plain TF32 products; 3: split operands, close to FP32 accuracy
         self.tc_terms = int(tc_terms)
+        # FP32 factors: applied from the FP32 fronts or from a BF16 copy
+        if storage not in ('fp32', 'bf16'):
+            raise ValueError("'Factor Storage' must be 'fp32' or 'bf16'")
+        self.storage = storage
         # grid cells at which nested dissection stops splitting a box
         self.leaf_cells = leaf_cells
         self.inverse = inverse
