@@ -229,3 +229,32 @@ def test_dataflow_wait_times_out_and_reports():
     fac.apply(again)
     eng.check()
     assert torch.allclose(again, good, rtol=1e-12, atol=1e-12 * float(good.abs().max()))
+
+
+@pytest.mark.parametrize('shape,params', [((48, 48, 1), {'Reynolds Number': 2000}),
+                                          ((24, 20, 1), {'Problem Type': 'Differentially Heated Cavity',
+                                                         'Rayleigh Number': 1e5, 'Prandtl Number': 1000,
+                                                         'Reynolds Number': 1, 'Grid Stretching Factor': 1.5}),
+                                          ((10, 10, 8), {'Reynolds Number': 300})])
+def test_fp32_inner_products_with_fp64_refinement(shape, params):
+    """Mixed-precision Krylov: FP32 factors, Arnoldi products with an FP32
+    copy of the gauged Jacobian, FP64 residuals between cycles -- the solve
+    still meets the FP64 tolerance and matches the all-FP64-operator solve."""
+    from transiflow_gb300 import Interface
+    nx, ny, nz = shape
+    ys = []
+    for inner in ('fp64', 'fp32'):
+        p = dict(params)
+        p['CUDA'] = {'Factor Precision': 'fp32', 'Tolerance': 1e-12, 'Inner Precision': inner}
+        itf = Interface(p, nx, ny, nz)
+        rng = np.random.default_rng(11)
+        x = itf.vector_from_array(0.5 * rng.standard_normal(itf.n))
+        J = itf.jacobian(x)
+        b = rng.standard_normal(itf.n)
+        y = itf.solve(J, itf.vector_from_array(b)).numpy()
+        A = _gauged(J.to_scipy(), itf.dim)
+        bg = b.copy()
+        bg[itf.dim] = 0
+        assert np.linalg.norm(A @ y - bg) / np.linalg.norm(bg) < 1e-11
+        ys.append(y)
+    assert np.linalg.norm(ys[1] - ys[0]) / np.linalg.norm(ys[0]) < 1e-9

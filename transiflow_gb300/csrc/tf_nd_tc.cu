@@ -29,6 +29,7 @@
 // its tensor memory.
 
 #include "tf_nd.cuh"
+#include "tf_tcgen05.cuh"
 
 namespace tf {
 namespace nd {
@@ -55,21 +56,11 @@ static_assert(TC_BM * TC_EPI_STRIDE * 4 <= TC_STAGES * (TC_A_BYTES + TC_B_BYTES)
 constexpr uint32_t TC_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
                               ((uint32_t)(TC_BM >> 4) << 24);
 
-// Shared-memory matrix descriptor of a K-major operand with the 128-byte
-// swizzle: 8-row groups of 128-byte rows, 1024 bytes apart (SBO), leading
-// byte offset unused (1), descriptor version 1 (bits 46-47), layout type
-// SWIZZLE_128B = 2 (bits 61-63).  The start address advances by 32 bytes per
-// K step of 8 TF32 values inside the swizzle row.
-__device__ __forceinline__ uint64_t sw128_desc(unsigned saddr) {
-    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
+using namespace tc5;
 
 // Byte offset of FP32 element (row, q), q < 32, in a 128-byte-swizzled
 // K-major tile whose base is 1024-byte aligned.
-__device__ __forceinline__ unsigned sw128_off(int row, int q) {
-    return (unsigned)(row * 128 + ((((q >> 2) ^ (row & 7)) & 7) << 4) + (q & 3) * 4);
-}
+__device__ __forceinline__ unsigned sw128_off(int row, int q) { return sw128_piece(row, q >> 2) + (q & 3) * 4; }
 
 __device__ __forceinline__ uint32_t to_tf32(float v) {
     uint32_t r;
@@ -77,49 +68,10 @@ __device__ __forceinline__ uint32_t to_tf32(float v) {
     return r;
 }
 
-__device__ __forceinline__ void sts_u32(unsigned addr, uint32_t v) {
-    asm volatile("st.shared.u32 [%0], %1;\n" ::"r"(addr), "r"(v) : "memory");
-}
-
-__device__ __forceinline__ unsigned tc_smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ bool tc_wait(uint64_t *bar, unsigned parity) {
-    const unsigned a = tc_smem_u32(bar);
-    for (int it = 0; it < (1 << 22); ++it) {
-        unsigned ok;
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-                     : "=r"(ok) : "r"(a), "r"(parity) : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
 __device__ __forceinline__ void tc_mma(unsigned tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, bool acc) {
     asm volatile("{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
                  " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
                  ::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"((unsigned)acc) : "memory");
-}
-
-__device__ __forceinline__ void tc_commit(uint64_t *bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n"
-                 ::"r"(tc_smem_u32(bar)) : "memory");
-}
-
-// 32 consecutive FP32 columns of this thread's tensor-memory lane.
-__device__ __forceinline__ void tc_ld32(unsigned taddr, float *v) {
-    uint32_t r[32];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                   "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-                   "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 template <int TERMS>
@@ -138,17 +90,17 @@ __global__ void __launch_bounds__(TC_THREADS, TERMS == 1 ? 2 : 1)
     if (w <= 0 || r0 >= f || c0 >= f) return;
     float *F = fronts + P.front_off[node];
     unsigned char *smem = reinterpret_cast<unsigned char *>(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
-    const unsigned sbase = tc_smem_u32(smem);
+    const unsigned sbase = smem_addr(smem);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (tid == 0) {
         for (int s = 0; s <= TC_STAGES; ++s)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(tc_smem_u32(&bar[s])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&bar[s])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
-                     ::"r"(tc_smem_u32(&tmem_slot)), "r"((unsigned)TC_BN) : "memory");
+                     ::"r"(smem_addr(&tmem_slot)), "r"((unsigned)TC_BN) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -184,7 +136,7 @@ __global__ void __launch_bounds__(TC_THREADS, TERMS == 1 ? 2 : 1)
         }
         // the stage is free once the MMAs of chunk c - TC_STAGES are done
         // (waited for after this chunk's loads are in flight)
-        if (c >= TC_STAGES && !tc_wait(&bar[s], (unsigned)((c / TC_STAGES - 1) & 1))) ok = false;
+        if (c >= TC_STAGES && !wait_parity(&bar[s], (unsigned)((c / TC_STAGES - 1) & 1))) ok = false;
 #pragma unroll
         for (int i = 0; i < TC_BM / 8; ++i) {
             const int row = warp * (TC_BM / 8) + i;
@@ -215,13 +167,13 @@ __global__ void __launch_bounds__(TC_THREADS, TERMS == 1 ? 2 : 1)
                     tc_mma(tmem, sw128_desc(As + kk * 32), sw128_desc(Bs + kk * 32), TC_IDESC, (c | kk) != 0);
                 }
             }
-            tc_commit(&bar[s]);
+            commit(&bar[s]);
         }
     }
-    if (tid == 0) tc_commit(&bar[TC_STAGES]);
-    if (!tc_wait(&bar[TC_STAGES], 0u)) {
+    if (tid == 0) commit(&bar[TC_STAGES]);
+    if (!wait_parity(&bar[TC_STAGES], 0u)) {
         ok = false;
-        tc_wait(&bar[TC_STAGES], 0u);
+        wait_parity(&bar[TC_STAGES], 0u);
     }
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     ok = __syncthreads_and(ok);
@@ -239,7 +191,7 @@ __global__ void __launch_bounds__(TC_THREADS, TERMS == 1 ? 2 : 1)
             for (int h = 0; h < 2; ++h) {
                 const int col = (warp >> 2) * 64 + h * 32;   // within the pass
                 float v[32];
-                tc_ld32(tmem + ((unsigned)(lg * 32) << 16) + (unsigned)(pass * TC_EPI_COLS + col), v);
+                tmem_ld32(tmem + ((unsigned)(lg * 32) << 16) + (unsigned)(pass * TC_EPI_COLS + col), v);
 #pragma unroll
                 for (int i = 0; i < 32; i += 4)
                     *reinterpret_cast<float4 *>(Cs + row * TC_EPI_STRIDE + col + i) =

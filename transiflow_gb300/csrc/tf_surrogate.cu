@@ -3,7 +3,7 @@
 // pseudo-arclength continuation.  Activations are channels-last
 // ([cell][channel], cell = i + nx*(j + ny*k), the ordering of the state
 // vector), operands are BF16 and every product is accumulated in FP32 on the
-// tensor cores (mma.sync m16n8k16).  Training runs here too: the gradient
+// tensor cores (tcgen05.mma with tensor-memory accumulators).  Training runs here too: the gradient
 // with respect to the input of a layer is the same convolution with the
 // mirrored, transposed weights; the weight gradient is an FP32 reduction over
 // cells written as per-chunk partial sums and reduced in a fixed order, so a
@@ -20,11 +20,11 @@
 #include <cuda_bf16.h>
 
 #include "tf_common.cuh"
+#include "tf_tcgen05.cuh"
 
 namespace tf {
 namespace sg {
 
-constexpr int CONV_WARPS = 4;     // 16 cells per warp, 64 per CTA
 constexpr int WG_CELLS = 1024;    // cells per weight-gradient chunk
 constexpr int WG_SUB = 32;        // cells staged in shared memory at a time
 constexpr int WG_THREADS = 256;
@@ -40,20 +40,6 @@ struct StateScales {
     double a[MAX_DOF];
 };
 
-__device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16 *p) {
-    return __ldg(reinterpret_cast<const unsigned int *>(p));
-}
-
-// D = A * B + D, A 16x16 (row), B 16x8 (col), BF16 operands, FP32 accumulators.
-__device__ __forceinline__ void mma_bf16(float c[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                         uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
 // Neighbour of cell (i, j, k) across tap, or -1 outside the grid (zero padding).
 __device__ __forceinline__ int neighbour(int i, int j, int k, int tap, int nx, int ny, int nz) {
     const int a = i + tap % 3 - 1, b = j + (tap / 3) % 3 - 1, c = k + tap / 9 - 1;
@@ -61,65 +47,144 @@ __device__ __forceinline__ int neighbour(int i, int j, int k, int tap, int nx, i
     return a + nx * (b + ny * c);
 }
 
-// One 3x3x3 convolution as an implicit GEMM: rows are cells, K runs over
-// (tap, input channel), N over output channels.  A warp owns 16 consecutive
-// cells and all NP output channels.  Lane (g = lane/4, t = lane%4) holds the
-// A fragment of cells base+g and base+g+8 at input channels 2t, 2t+1, 2t+8,
-// 2t+9 of each 16-channel chunk, and the B fragment of output channel g at
-// the same input channels.  Z (FP32, optional) receives conv + bias, A (BF16,
-// optional) relu(conv + bias) when relu is set, else conv + bias.
-template <int KC, int NT>
-__global__ void __launch_bounds__(32 * CONV_WARPS)
+// One 3x3x3 convolution as an implicit GEMM on the tensor cores: rows (M) are
+// 128 consecutive cells per CTA, N the NP output channels, K runs over (tap,
+// input channel) in chunks of 64 BF16 values -- one 128-byte swizzle row,
+// 64 / KP taps of KP channels (27 taps: 14 chunks at KP = 32, 7 at KP = 16,
+// the last one padded with zeros).  The weights of every chunk stay in
+// shared memory for the whole CTA (B, K-major: B[tap][n][k] is already K
+// contiguous); each chunk of A is gathered by the CTA's 128 threads, one
+// cell each (eight 16-byte loads of the neighbour cells' channels, zero
+// outside the grid), into one of two swizzled stages while the tensor cores
+// work on the other.  One thread issues tcgen05.mma (kind::f16, BF16
+// operands, M = 128, N = NP, K = 16 per instruction) accumulating in FP32 in
+// tensor memory; the epilogue reads each cell's NP accumulators
+// (tcgen05.ld), adds the bias and writes Z (FP32, conv + bias) and A (BF16,
+// relu(conv + bias) when relu is set, else conv + bias).  A bounded wait that
+// gives up leaves Z and A filled with NaN for the CTA's cells (the training
+// loss or the prediction then shows it) instead of hanging.
+constexpr int CV_M = 128;          // cells per CTA = tensor-memory lanes
+constexpr int CV_THREADS = 128;    // one thread per cell
+constexpr int CV_STAGES = 2;
+
+template <int KP, int NP>
+struct ConvShape {
+    static constexpr int taps = 64 / KP;                        // taps per K chunk
+    static constexpr int chunks = (27 + taps - 1) / taps;
+    static constexpr int b_chunk = NP * 128;                    // bytes of B per chunk
+    static constexpr int b_bytes = chunks * b_chunk;
+    static constexpr int a_stage = CV_M * 128;
+    static constexpr size_t smem = (size_t)b_bytes + CV_STAGES * a_stage + 1024;
+    // kind::f16 instruction descriptor: D FP32, A and B BF16, both K-major,
+    // N >> 3 at bit 17, M >> 4 at bit 24
+    static constexpr uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NP >> 3) << 17) |
+                                      ((uint32_t)(CV_M >> 4) << 24);
+};
+
+__device__ __forceinline__ void mma_bf16_tc(unsigned tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, bool acc) {
+    asm volatile("{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                 ::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"((unsigned)acc) : "memory");
+}
+
+template <int KP, int NP>
+__global__ void __launch_bounds__(CV_THREADS)
 conv_kernel(int nx, int ny, int nz, const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restrict__ B,
             const float *__restrict__ bias, float *__restrict__ Z, __nv_bfloat16 *__restrict__ A, int relu) {
-    constexpr int KP = 16 * KC, NP = 8 * NT;
+    using namespace tc5;
+    using S = ConvShape<KP, NP>;
+    extern __shared__ unsigned char cv_raw[];
+    __shared__ __align__(8) uint64_t bar[CV_STAGES + 1];
+    __shared__ unsigned tmem_slot;
     const int ncell = nx * ny * nz;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane >> 2, t = lane & 3;
-    const int base = (blockIdx.x * CONV_WARPS + warp) * 16;
-    if (base >= ncell) return;  // the whole warp leaves: mma.sync needs all 32 lanes
-    const int r0 = base + g, r1 = base + g + 8;
-    const bool v0 = r0 < ncell, v1 = r1 < ncell;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    unsigned char *smem = reinterpret_cast<unsigned char *>(((uintptr_t)cv_raw + 1023) & ~(uintptr_t)1023);
+    const unsigned sb = smem_addr(smem);          // B, chunk after chunk
+    const unsigned sa = sb + S::b_bytes;          // A stages
+    if (tid == 0) {
+        for (int s = 0; s <= CV_STAGES; ++s) mbar_init1(&bar[s]);
+        mbar_init_fence();
+    }
+    if (warp == 0) tmem_alloc(&tmem_slot, 32);
+    // the weights of every chunk: 16-byte piece p of row n of chunk c holds
+    // input channels 8p .. 8p + 7 of the chunk's taps
+    constexpr int BPIECES = S::chunks * NP * 8;
+    for (int q = tid; q < BPIECES; q += CV_THREADS) {
+        const int c = q / (NP * 8), rem = q % (NP * 8), n = rem >> 3, p = rem & 7;
+        const int tap = c * S::taps + (8 * p) / KP, ci = (8 * p) % KP;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (tap < 27) v = __ldg(reinterpret_cast<const uint4 *>(B + ((size_t)tap * NP + n) * KP + ci));
+        sts_v4(sb + c * S::b_chunk + sw128_piece(n, p), v);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const unsigned tmem = tmem_slot;
+    const int cell = blockIdx.x * CV_M + tid;
+    const bool valid = cell < ncell;
     const int nxy = nx * ny;
-    const int i0 = r0 % nx, j0 = (r0 / nx) % ny, k0 = r0 / nxy;
-    const int i1 = r1 % nx, j1 = (r1 / nx) % ny, k1 = r1 / nxy;
-    float acc[NT][4];
+    const int ci0 = valid ? cell % nx : 0, cj0 = valid ? (cell / nx) % ny : 0, ck0 = valid ? cell / nxy : 0;
+    bool ok = true;
+    for (int c = 0; c < S::chunks; ++c) {
+        const int s = c % CV_STAGES;
+        const unsigned As = sa + s * S::a_stage;
+        uint4 v[8];
 #pragma unroll
-    for (int nt = 0; nt < NT; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-    for (int tap = 0; tap < 27; ++tap) {
-        const int n0 = v0 ? neighbour(i0, j0, k0, tap, nx, ny, nz) : -1;
-        const int n1 = v1 ? neighbour(i1, j1, k1, tap, nx, ny, nz) : -1;
-        const __nv_bfloat16 *x0 = X + (size_t)(n0 < 0 ? 0 : n0) * KP + 2 * t;
-        const __nv_bfloat16 *x1 = X + (size_t)(n1 < 0 ? 0 : n1) * KP + 2 * t;
-        const __nv_bfloat16 *bt = B + ((size_t)tap * NP + g) * KP + 2 * t;
+        for (int p = 0; p < 8; ++p) {
+            const int tap = c * S::taps + (8 * p) / KP, ch = (8 * p) % KP;
+            const int nb = (valid && tap < 27) ? neighbour(ci0, cj0, ck0, tap, nx, ny, nz) : -1;
+            v[p] = nb >= 0 ? __ldg(reinterpret_cast<const uint4 *>(X + (size_t)nb * KP + ch))
+                           : make_uint4(0u, 0u, 0u, 0u);
+        }
+        // the stage is free once the MMAs of chunk c - CV_STAGES are done
+        if (c >= CV_STAGES && !wait_parity(&bar[s], (unsigned)((c / CV_STAGES - 1) & 1))) ok = false;
 #pragma unroll
-        for (int kc = 0; kc < KC; ++kc) {
-            const uint32_t a0 = n0 >= 0 ? ld_pair(x0 + 16 * kc) : 0u;
-            const uint32_t a1 = n1 >= 0 ? ld_pair(x1 + 16 * kc) : 0u;
-            const uint32_t a2 = n0 >= 0 ? ld_pair(x0 + 16 * kc + 8) : 0u;
-            const uint32_t a3 = n1 >= 0 ? ld_pair(x1 + 16 * kc + 8) : 0u;
+        for (int p = 0; p < 8; ++p) sts_v4(As + sw128_piece(tid, p), v[p]);
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
 #pragma unroll
-            for (int nt = 0; nt < NT; ++nt) {
-                const __nv_bfloat16 *bp = bt + (size_t)nt * 8 * KP + 16 * kc;
-                mma_bf16(acc[nt], a0, a1, a2, a3, ld_pair(bp), ld_pair(bp + 8));
+            for (int kk = 0; kk < 4; ++kk)
+                mma_bf16_tc(tmem, sw128_desc(As + kk * 32), sw128_desc(sb + c * S::b_chunk + kk * 32), S::idesc,
+                            (c | kk) != 0);
+            commit(&bar[s]);
+        }
+    }
+    if (tid == 0) commit(&bar[CV_STAGES]);
+    if (!wait_parity(&bar[CV_STAGES], 0u)) {
+        ok = false;
+        wait_parity(&bar[CV_STAGES], 0u);
+    }
+    fence_after();
+    ok = __syncthreads_and(ok);
+    float acc[NP];
+    const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16);
+    if (NP == 32) tmem_ld32(taddr, acc);
+    else tmem_ld16(taddr, acc);
+    if (valid) {
+        const float qnan = __int_as_float(0x7fc00000);
+#pragma unroll
+        for (int col = 0; col < NP; col += 4) {
+            float z[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) z[u] = ok ? acc[col + u] + (bias ? bias[col + u] : 0.f) : qnan;
+            if (Z) *reinterpret_cast<float4 *>(Z + (size_t)cell * NP + col) = make_float4(z[0], z[1], z[2], z[3]);
+            if (A) {
+                float y[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) y[u] = relu ? fmaxf(z[u], 0.f) : z[u];
+                __nv_bfloat162 *ap = reinterpret_cast<__nv_bfloat162 *>(A + (size_t)cell * NP + col);
+                ap[0] = __floats2bfloat162_rn(y[0], y[1]);
+                ap[1] = __floats2bfloat162_rn(y[2], y[3]);
             }
         }
     }
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-        const int col = nt * 8 + 2 * t;
-        const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int r = h ? r1 : r0;
-            if (!(h ? v1 : v0)) continue;
-            const float z0 = acc[nt][2 * h] + b0, z1 = acc[nt][2 * h + 1] + b1;
-            if (Z) *reinterpret_cast<float2 *>(Z + (size_t)r * NP + col) = make_float2(z0, z1);
-            if (A) {
-                const float y0 = relu ? fmaxf(z0, 0.f) : z0, y1 = relu ? fmaxf(z1, 0.f) : z1;
-                *reinterpret_cast<__nv_bfloat162 *>(A + (size_t)r * NP + col) = __floats2bfloat162_rn(y0, y1);
-            }
-        }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        tmem_free(tmem, 32);
     }
 }
 
@@ -320,6 +385,21 @@ static inline bool grid_ok(int nx, int ny, int nz) {
 
 static inline int nchunks(int ncell) { return (ncell + WG_CELLS - 1) / WG_CELLS; }
 
+template <int KP, int NP>
+static int launch_conv(int ncell, int nx, int ny, int nz, const __nv_bfloat16 *x, const __nv_bfloat16 *w,
+                       const float *bias, float *z, __nv_bfloat16 *a, int relu, cudaStream_t s) {
+    const size_t sm = ConvShape<KP, NP>::smem;
+    if (sm > 48 * 1024 &&
+        cudaFuncSetAttribute((const void *)conv_kernel<KP, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sm) != cudaSuccess) {
+        cudaGetLastError();
+        return TF_ERR_CUDA;
+    }
+    conv_kernel<KP, NP><<<blocks(ncell, CV_M), CV_THREADS, sm, s>>>(nx, ny, nz, x, w, bias, z, a, relu);
+    launched();
+    return TF_OK;
+}
+
 }  // namespace sg
 }  // namespace tf
 
@@ -330,18 +410,16 @@ extern "C" int tf_sg_conv(int nx, int ny, int nz, int kp, int np, const void *d_
                           const float *d_bias, float *d_z, void *d_a, int relu, tf_stream_t stream) {
     if (!grid_ok(nx, ny, nz) || !ch_ok(kp) || !ch_ok(np) || !d_x || !d_w || (!d_z && !d_a)) return TF_ERR_ARG;
     const int ncell = nx * ny * nz;
-    const int grid = blocks(ncell, 16 * CONV_WARPS);
     const auto *x = static_cast<const __nv_bfloat16 *>(d_x);
     const auto *w = static_cast<const __nv_bfloat16 *>(d_w);
     auto *a = static_cast<__nv_bfloat16 *>(d_a);
     cudaStream_t s = (cudaStream_t)stream;
-    const int threads = 32 * CONV_WARPS;
-    if (kp == 16 && np == 16) conv_kernel<1, 2><<<grid, threads, 0, s>>>(nx, ny, nz, x, w, d_bias, d_z, a, relu);
-    else if (kp == 16) conv_kernel<1, 4><<<grid, threads, 0, s>>>(nx, ny, nz, x, w, d_bias, d_z, a, relu);
-    else if (np == 16) conv_kernel<2, 2><<<grid, threads, 0, s>>>(nx, ny, nz, x, w, d_bias, d_z, a, relu);
-    else conv_kernel<2, 4><<<grid, threads, 0, s>>>(nx, ny, nz, x, w, d_bias, d_z, a, relu);
-    launched();
-    return cuda_status();
+    int e;
+    if (kp == 16 && np == 16) e = launch_conv<16, 16>(ncell, nx, ny, nz, x, w, d_bias, d_z, a, relu, s);
+    else if (kp == 16) e = launch_conv<16, 32>(ncell, nx, ny, nz, x, w, d_bias, d_z, a, relu, s);
+    else if (np == 16) e = launch_conv<32, 16>(ncell, nx, ny, nz, x, w, d_bias, d_z, a, relu, s);
+    else e = launch_conv<32, 32>(ncell, nx, ny, nz, x, w, d_bias, d_z, a, relu, s);
+    return e ? e : cuda_status();
 }
 
 extern "C" size_t tf_sg_wgrad_workspace_bytes(int ncell, int kp, int np) {

@@ -55,6 +55,12 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       factorisation the entries the preconditioner reads are
                       rounded to a BF16 copy, and every application reads
                       that copy (half the bytes) with FP32 products and sums
+  'Inner Precision'   'fp64' (default) or 'fp32': the Arnoldi products of
+                      FGMRES use an FP32 copy of the gauged Jacobian (SpMV in
+                      FP32 values, FP64 vectors); every restart cycle stops
+                      after gaining six digits and the next starts from the
+                      FP64 residual (iterative refinement), so the solve still
+                      meets 'Tolerance' in FP64
   'Leaf Cells'        grid cells of a box at which nested dissection stops
                       splitting (default 48)
   'CUDA Graphs'       replay the factorisation and solve launch sequences from
@@ -225,7 +231,8 @@ class Interface(_Base):
                              tc_min_front=(int(opts.get('Tensor Core Min Front', 1024))
                                            if opts.get('Tensor Cores', True) else 0),
                              tc_terms=1 if opts.get('Tensor Core Precision', 'tf32x3') == 'tf32' else 3,
-                             storage=opts.get('Factor Storage', 'fp32'))
+                             storage=opts.get('Factor Storage', 'fp32'),
+                             inner=opts.get('Inner Precision', 'fp64'))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

@@ -340,7 +340,7 @@ class Solver:
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
                  reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True, flow=False,
                  flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48, sweep=False, tc_min_front=1024,
-                 tc_terms=3, storage='fp32'):
+                 tc_terms=3, storage='fp32', inner='fp64'):
         self.itf = interface
         # FP32 factorisations: heights whose widest front has at least this
         # many rows use blocked rank-256 tensor-core updates (0: never)
@@ -351,6 +351,12 @@ class Solver:
         if storage not in ('fp32', 'bf16'):
             raise ValueError("'Factor Storage' must be 'fp32' or 'bf16'")
         self.storage = storage
+        # precision of the Arnoldi operator products: the FP64 Jacobian, or an
+        # FP32 copy inside cycles whose FP64 residuals refine the solution
+        if inner not in ('fp64', 'fp32'):
+            raise ValueError("'Inner Precision' must be 'fp64' or 'fp32'")
+        self.inner = inner
+        self._opbuf32 = None
         # grid cells at which nested dissection stops splitting a box
         self.leaf_cells = leaf_cells
         self.inverse = inverse
@@ -528,6 +534,11 @@ class Solver:
             self._opbuf_src = None
         if self._opbuf_src is not op:
             self._copy(op.values, self._opbuf)
+            if self.inner == 'fp32':
+                if self._opbuf32 is None or self._opbuf32.numel() != op.values.numel():
+                    self._opbuf32 = torch.empty(op.values.numel(), dtype=torch.float32, device=op.values.device)
+                _lib.check(_lib.load().tf_vec_to_f32(op.values.numel(), op.values.data_ptr(),
+                                                     self._opbuf32.data_ptr(), _stream()), 'tf_vec_to_f32')
             self._opbuf_src = op
         key = (fac.precision, j)
         step = self._steps.get(key)
@@ -540,13 +551,17 @@ class Solver:
             lib = _lib.load()
             pat = op.jac.pattern
             opbuf = self._opbuf
+            # inner products with the FP32 copy of the operator ('Inner
+            # Precision' fp32) or the FP64 operator itself
+            spmv = lib.tf_spmv_f32 if self.inner == 'fp32' else lib.tf_spmv_f64
+            opvals = self._opbuf32 if self.inner == 'fp32' else opbuf
 
             def fn():
                 self._copy(V[j], eng.vec)
                 eng.solve_raw()
                 self._copy(eng.vec, Z[j])
-                _lib.check(lib.tf_spmv_f64(op.n, pat.rowptr.data_ptr(), pat.cols.data_ptr(), opbuf.data_ptr(),
-                                           Z[j].data_ptr(), w.data_ptr(), 1.0, 0.0, _stream()), 'tf_spmv_f64')
+                _lib.check(spmv(op.n, pat.rowptr.data_ptr(), pat.cols.data_ptr(), opvals.data_ptr(),
+                                Z[j].data_ptr(), w.data_ptr(), 1.0, 0.0, _stream()), 'tf_spmv')
                 self._mdot_into(V, j + 1, w, h)
                 self._mgs(V, j + 1, h, w)
                 self._mdot_into(V, j + 1, w, h2)
@@ -581,6 +596,7 @@ class Solver:
         its = 0
         relres = 1.0
         tmp = torch.empty_like(b)
+        inner_gain = 1e-6 if self.inner == 'fp32' else 0.0
         while its < maxit:
             beta = self._norm(r)
             relres = beta / bn
@@ -616,7 +632,10 @@ class Solver:
                 g[j] = cs[j] * g[j]
                 its += 1
                 k = j + 1
-                if abs(g[j + 1]) <= self.tol * bn or its >= maxit or hn == 0:
+                # with FP32 inner products a cycle can only gain about six
+                # digits on its own starting residual; the FP64 residual below
+                # then starts the next cycle (iterative refinement)
+                if abs(g[j + 1]) <= max(self.tol * bn, inner_gain * beta) or its >= maxit or hn == 0:
                     break
             if k:
                 R = np.zeros((k, k))
