@@ -85,7 +85,7 @@ def parse():
     ap.add_argument('--reuse-its', type=int, default=None, help="'Reuse Iterations' (default: the backend's)")
     ap.add_argument('--reuse-drift', type=float, default=None, help="'Reuse Drift' (default: the backend's)")
     ap.add_argument('--no-tc', action='store_true', help='FP32 factors without tensor-core updates')
-    ap.add_argument('--profile', default=None, choices=['factor', 'solve', 'assemble', 'tc'],
+    ap.add_argument('--profile', default=None, choices=['factor', 'solve', 'assemble', 'tc', 'spmv', 'conv'],
                     help='run only a few launches of one stage (for ncu captures)')
     ap.add_argument('--nz', type=int, default=None, help='--profile: cells in z (1: the 2D grid)')
     ap.add_argument('--re', type=float, default=1000.0, help='Reynolds number of the --profile state')
@@ -235,6 +235,7 @@ def train_predictor(args):
     from transiflow_gb300.surrogate import Recorder, Surrogate
     t0 = time.perf_counter()
     groups = []
+    stalls = []
     for n in [int(v) for v in args.train_grids.split(',')]:
         for seed in [int(v) for v in args.train_seeds.split(',')]:
             itf = Interface({'CUDA': solver_options(args, 'fp32')}, n, n, n)
@@ -250,7 +251,15 @@ def train_predictor(args):
             # substitution makes the secant tangent useless), later steps at
             # most --train-ds so that the branch yields many points
             ds = args.ds * float(np.random.default_rng(seed).uniform(0.8, 1.2))
-            cont.continuation(x0, 'Reynolds Number', 0.0, args.train_target, ds, ds_max=args.train_ds)
+            try:
+                cont.continuation(x0, 'Reynolds Number', 0.0, args.train_target, ds, ds_max=args.train_ds)
+            except Exception as e:
+                # a singular point before the target (on the 32^3 branch near
+                # Re 2338 the corrector cannot converge at any step size):
+                # the branch ends there, its points so far are kept
+                if 'stalled' not in str(e):
+                    raise
+                stalls.append((n, seed, float(itf.get_parameter('Reynolds Number'))))
             groups.append(((n, n, n), rec.samples))
             del itf, cont, x0
             _free()
@@ -263,8 +272,13 @@ def train_predictor(args):
         for dims, g in groups:
             if g:
                 losses.append(float(net.train(g, dims, steps=args.train_steps, lr=2e-3, batch=4, seed=r)[-1]))
+    # the step-size proposal: the network's error relative to the secant
+    # predictor and the secant error plain steps handled comfortably
+    step_model = net.calibrate_steps([(dims, g) for dims, g in groups if g])
     torch.cuda.synchronize()
     info = {'branches': len(groups), 'points': sum(len(g) for _, g in groups), 'branches_s': branches_s,
+            'step_model': step_model,
+            'ended_at_singular_point': stalls,
             'train_s': time.perf_counter() - t1, 'adam_steps': args.train_rounds * args.train_steps * len(groups),
             'final_loss': losses[-1] if losses else None, 'parameters': net.parameters()}
     return net, info
@@ -351,6 +365,7 @@ def learned_arm(args, net, rank, local):
            'branch': {'points': cont.stats['points'], 'rhs': cont.stats['rhs'], 'jacobian': cont.stats['jacobian'],
                       'solve': cont.stats['solve'], 'learned_accepted': cont.stats['learned_accepted'],
                       'learned_rejected': cont.stats['learned_rejected'], 'per_step_solver': per,
+                      'steps_proposed': pred.steps_proposed,
                       'mus': [r['mu'] for r in logs[-1]], 'step_s': t_dev}}
     out['end_state'] = _polish(itf, x, mu)
     return out, itf
@@ -772,12 +787,46 @@ def profile_stage(args):
     s = 0.1 * np.random.default_rng(1).standard_normal(itf.n)
     x = itf.vector_from_array(s)
     J = itf.jacobian(x)
-    t0 = time.perf_counter()
-    fac = itf.solver.factorization(J)
-    torch.cuda.synchronize()
-    first = time.perf_counter() - t0
+    fac, first = None, None
+    if args.profile in ('factor', 'solve', 'tc'):
+        # only these stages hold the frontal matrices on the device
+        t0 = time.perf_counter()
+        fac = itf.solver.factorization(J)
+        torch.cuda.synchronize()
+        first = time.perf_counter() - t0
     st = torch.cuda.current_stream()
     times = []
+    if args.profile in ('spmv', 'conv'):
+        from transiflow_gb300 import _lib
+        from transiflow_gb300.vector import _stream
+        lib = _lib.load()
+        if args.profile == 'spmv':
+            rp, cp = itf.pattern.rowptr, itf.pattern.cols
+            y = torch.empty_like(x.data)
+
+            def run():
+                _lib.check(lib.tf_spmv_f64(itf.n, rp.data_ptr(), cp.data_ptr(), J.values.data_ptr(),
+                                           x.data.data_ptr(), y.data_ptr(), 1.0, 0.0, _stream()), 'tf_spmv_f64')
+        else:
+            # one forward pass of the learned predictor's network on this grid
+            from transiflow_gb300.surrogate import Surrogate
+            net = Surrogate(itf.dof)
+            net.fit_scales([{'x0': x.data, 't': x.data, 'x1': x.data, 'mu': 1.0, 'ds': 1.0}])
+            dims = (itf.nx, itf.ny, itf.nz)
+
+            def run():
+                net.predict(x.data, x.data, 1.0, 1.0, dims)
+        run()
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            run()
+            e1.record(st)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1000.0)
+        print(json.dumps({'profile': args.profile, 'nx': args.nx, 'nz': args.nz, 's_per_call': times}))
+        return
     if args.profile == 'tc':
         # the tensor-core update alone on the widest height (scribbles on the
         # fronts; nothing is solved afterwards)
@@ -815,10 +864,13 @@ def profile_stage(args):
         e1.record(st)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1000.0)
+    out = {'profile': args.profile, 'nx': args.nx, 'nz': args.nz, 'unknowns': itf.n, 'precision': args.precision,
+           's_per_call': times}
     plan = itf.solver.plan
-    print(json.dumps({'profile': args.profile, 'nx': args.nx, 'nz': args.nz, 'unknowns': itf.n,
-                      'precision': args.precision, 's_per_call': times, 'first_factor_s': first,
-                      'factor_gflop': plan.flops / 1e9, 'front_gb': plan.front_elems * (8 if args.precision == 'fp64' else 4) / 1e9}))
+    if plan is not None:
+        out.update({'first_factor_s': first, 'factor_gflop': plan.flops / 1e9,
+                    'front_gb': plan.front_elems * (8 if args.precision == 'fp64' else 4) / 1e9})
+    print(json.dumps(out))
 
 
 def batched(args):

@@ -330,3 +330,73 @@ def test_surrogate_rejects_fields_its_kernels_cannot_read():
             check_field(torch.zeros(2 * n, dtype=torch.float64, device='cuda')[::2], n)
         with pytest.raises(ValueError, match='values'):
             check_field(torch.zeros(n + 1, dtype=torch.float64, device='cuda'), n)
+
+
+@pytest.mark.gpu
+def test_samples_from_two_grid_sizes_train_one_network():
+    """Recorder samples (device vectors) of two branches on grids of
+    different sizes: fit_scales equals NumPy RMS values over the concatenated
+    samples, and training steps run on each grid with finite losses."""
+    import contextlib
+    import io
+    from transiflow_gb300 import Continuation, Interface
+    from transiflow_gb300.surrogate import Recorder, Surrogate
+    groups = []
+    for n in (10, 14):
+        itf = Interface({'CUDA': {'Tolerance': 1e-10}}, n, n)
+        rec = Recorder()
+        cont = Continuation(itf, newton_tolerance=1e-8, predictor=rec.predictor, log=rec.log)
+        with contextlib.redirect_stdout(io.StringIO()):
+            cont.continuation(cont.newton(itf.vector()), 'Reynolds Number', 0.0, 600.0, 100.0)
+        assert len(rec.samples) >= 3
+        assert all(s['x0'].is_cuda and s['x0'].numel() == itf.n for s in rec.samples)
+        groups.append(((n, n, 1), rec.samples))
+    samples = [s for _, g in groups for s in g]
+    net = Surrogate(3)
+    net.fit_scales(samples)
+
+    def rms(key):
+        a = np.concatenate([s[key].cpu().numpy().reshape(-1, 3) for s in samples])
+        return np.sqrt((a ** 2).mean(axis=0))
+    xr, tr = rms('x0'), rms('t')
+    d = np.concatenate([((s['x1'] - s['x0'] - s['ds'] * s['t']) / s['ds'] ** 2).cpu().numpy().reshape(-1, 3)
+                        for s in samples])
+    dr = np.sqrt((d ** 2).mean(axis=0))
+    assert np.allclose(net.scales['sx'], 1.0 / xr, rtol=1e-6)
+    assert np.allclose(net.scales['st'], 1.0 / tr, rtol=1e-6)
+    assert np.allclose(net.scales['sd'], dr, rtol=1e-6)
+    for dims, g in groups:
+        losses = net.train(g, dims, steps=5, lr=1e-3, batch=2)
+        assert np.all(np.isfinite(losses))
+
+
+@pytest.mark.parametrize('quality', ['exact', 'wrong'])
+def test_predictor_can_propose_the_step_size(quality):
+    """A predictor returning (x, mu, ds') sets the step it is corrected on:
+    exact proposals of twice the step are accepted and the branch needs
+    fewer points; wrong ones are rejected and the step is redone from the
+    secant predictor with the original step, giving the plain branch."""
+    from transiflow_gb300.continuation import Continuation
+
+    def exact(interface, x0, mu0, dx, dmu, ds):
+        mu = mu0 + 2 * ds * dmu
+        r = np.roots([1, 0, 1, -mu]).real.max()
+        return np.array([r, 0.5 * mu]), mu, 2 * ds
+
+    def wrong(interface, x0, mu0, dx, dmu, ds):
+        return np.array([1e6, -1e6]), mu0 + ds * dmu, 3 * ds
+
+    plain = Continuation(_Cubic(), newton_tolerance=1e-10, quiet=True)
+    xp, mup = plain.continuation(np.zeros(2), 'mu', 0.0, 10.0, 0.5, ds_max=0.5)
+    cont = Continuation(_Cubic(), newton_tolerance=1e-10, quiet=True,
+                        predictor=exact if quality == 'exact' else wrong)
+    x, mu = cont.continuation(np.zeros(2), 'mu', 0.0, 10.0, 0.5, ds_max=0.5 if quality == 'wrong' else 1.0)
+    assert abs(mu - 10.0) < 1e-4
+    r = np.roots([1, 0, 1, -mu]).real.max()
+    assert np.allclose(x, [r, 0.5 * mu], rtol=1e-9, atol=1e-9)
+    if quality == 'exact':
+        assert cont.stats['learned_rejected'] == 0
+        assert cont.stats['points'] < plain.stats['points']
+    else:
+        assert cont.stats['learned_accepted'] == 0
+        assert cont.stats['points'] == plain.stats['points'] and mu == mup and np.array_equal(x, xp)

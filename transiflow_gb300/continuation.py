@@ -23,11 +23,14 @@ branch is a loop over steps that ends by landing on the target.
 Beyond the reference:
 
 * ``predictor``: a callable ``(interface, x0, mu0, dx, dmu, ds)`` returning a
-  proposed point ``(x, mu)`` or ``None``.  The learned surrogate of
+  proposed point ``(x, mu)``, a proposed point with its own step size
+  ``(x, mu, ds')`` (the point is then corrected on the arclength sphere of
+  radius ds'), or ``None``.  The learned surrogate of
   :mod:`transiflow_gb300.surrogate` plugs in here.  A proposal gets a
   corrector budget of ``learned_newton_iterations``; when the corrector does
   not converge within it, the same step is redone from the secant predictor
-  with the full budget.  Every accepted point is judged by the same corrector.
+  with the full budget and the original step size.  Every accepted point is
+  judged by the same corrector.
 * ``step_size``: a callable ``(interface, ds, iterations, ds_min, ds_max)``
   returning the next step size, replacing the Newton-count rule after
   accepted steps (failed attempts always halve by that rule).
@@ -262,7 +265,7 @@ class Continuation:
     # -- one step along the branch ------------------------------------------------------
     def _attempt(self, name, x0, mu0, dx, dmu, ds, proposal):
         if proposal is not None:
-            x, mu = proposal
+            x, mu = proposal[0], proposal[1]
             return self.correct(name, x, mu, x0, mu0, ds, self.learned_newton_iterations)
         return self.correct(name, x0 + ds * dx, mu0 + ds * dmu, x0, mu0, ds)
 
@@ -273,8 +276,12 @@ class Continuation:
         proposal = None
         if learned and self.predictor is not None:
             proposal = self.predictor(self.interface, x0, mu0, dx, dmu, ds)
+        secant_ds = ds
         while True:
-            res = self._attempt(name, x0, mu0, dx, dmu, ds, proposal)
+            step = ds
+            if proposal is not None and len(proposal) > 2:
+                step = math.copysign(min(max(abs(proposal[2]), ds_min), ds_max), ds)
+            res = self._attempt(name, x0, mu0, dx, dmu, step, proposal)
             # a corrected point must have moved in the parameter: the secant
             # tangent below divides by that change
             ok = res.converged and res.mu != mu0
@@ -282,9 +289,11 @@ class Continuation:
                 proposal = None
                 if ok:
                     self.stats['learned_accepted'] += 1
+                    ds = step
                 else:
                     # redo the same step from the secant predictor
                     self.stats['learned_rejected'] += 1
+                    ds = secant_ds
                     continue
             if ok:
                 break

@@ -71,25 +71,28 @@ class Recorder:
     """Collects training samples from a plain continuation: pass
     ``recorder.predictor`` as the continuation's predictor (it proposes
     nothing, so the secant predictor runs) and ``recorder.log`` as its log.
-    A sample is (x0, t, mu0, ds, x1): the state, tangent and parameter a
-    step started from, the step it was accepted with and the point it
-    converged to."""
+    A sample is (x0, t, mu0, ds, x1, its): the state, tangent and parameter a
+    step started from, the step it was accepted with, the point it converged
+    to and the corrector iterations it took."""
 
     def __init__(self):
         self.samples = []
         self._pending = None
         self._ds = None
+        self._its = None
 
     def predictor(self, interface, x0, mu0, dx, dmu, ds):
         if self._pending is not None and self._ds is not None:
             px, pt, pmu = self._pending
-            self.samples.append({'x0': px, 't': pt, 'mu': pmu, 'ds': self._ds, 'x1': _snapshot(x0)})
+            self.samples.append({'x0': px, 't': pt, 'mu': pmu, 'ds': self._ds, 'x1': _snapshot(x0),
+                                 'its': self._its})
         self._pending = (_snapshot(x0), _snapshot(dx), float(mu0))
         self._ds = None
         return None
 
     def log(self, record):
         self._ds = float(record['ds'])
+        self._its = record.get('newton_iterations')
 
 
 class Surrogate:
@@ -130,6 +133,8 @@ class Surrogate:
             self.wb.append(torch.empty(27 * kp * np_, dtype=torch.bfloat16, **dev))
         self.step = 0
         self.scales = None
+        # step-size model, set by calibrate_steps
+        self.step_model = None
         self._bufs = {}
         self.export_weights()
 
@@ -305,6 +310,46 @@ class Surrogate:
                                            b['lwork'].numel(), _stream()), 'tf_sg_loss')
         return out.cpu().numpy()
 
+    def calibrate_steps(self, groups, optimal_iterations=3, quantile=0.75):
+        """Fit the step-size proposal on training samples, given as
+        ``[(dims, samples), ...]``.  For every sample the RMS errors of the
+        secant predictor (e_s) and of the learned predictor (e_l) against the
+        converged point are measured; ``eps`` is the given quantile of
+        e_l / e_s (how much of the secant error the network removes, read
+        conservatively), ``target`` the median secant error of the steps whose
+        corrector took at most ``optimal_iterations`` iterations (the error a
+        plain step is comfortable with).  Returns the model."""
+        ratios, comfortable, all_es = [], [], []
+        for dims, g in groups:
+            for smp in g:
+                smp = self._on_device(smp)
+                xs = smp['x0'] + smp['ds'] * smp['t']
+                xl = self.predict(smp['x0'], smp['t'], smp['mu'], smp['ds'], dims)
+                es = float((smp['x1'] - xs).pow(2).mean().sqrt())
+                el = float((smp['x1'] - xl).pow(2).mean().sqrt())
+                if es > 0:
+                    ratios.append(el / es)
+                    all_es.append(es)
+                    if smp.get('its') is not None and smp['its'] <= optimal_iterations:
+                        comfortable.append(es)
+        if not ratios:
+            raise ValueError('no samples with a nonzero secant error')
+        self.step_model = {'eps': float(np.quantile(ratios, quantile)),
+                           'target': float(np.median(comfortable if comfortable else all_es))}
+        return self.step_model
+
+    def propose_step(self, x, t, ds, correction_rms):
+        """The step at which the learned predictor's expected error, eps *
+        c * ds'^2 with the curvature c = correction_rms / ds^2 the network
+        predicts, equals the comfortable secant error; the ratio to ds stays
+        within [1/2, 2] (the bounds of the Newton-count rule)."""
+        sm = self.step_model
+        if sm is None or correction_rms <= 0 or not math.isfinite(correction_rms):
+            return ds
+        c = correction_rms / (ds * ds)
+        s = math.sqrt(sm['target'] / (sm['eps'] * c))
+        return ds * min(max(s / abs(ds), 0.5), 2.0)
+
     # -- inference ------------------------------------------------------------------
     def predict(self, x, t, mu, ds, dims):
         """The learned predictor x + ds t + correction (FP64 tensor)."""
@@ -322,15 +367,31 @@ class Surrogate:
 
 class LearnedPredictor:
     """The continuation's ``predictor`` hook over a trained surrogate: the
-    state from the network, the parameter from the secant."""
+    state from the network, the parameter from the secant, and -- once
+    ``Surrogate.calibrate_steps`` has run and ``propose_steps`` is set -- the
+    step size: the network's predicted correction of the secant predictor
+    gives the branch's curvature, from which ``Surrogate.propose_step``
+    picks the step (the network then predicts again at that step).  The
+    reference picks steps by Newton counts only (Continuation.py:197-209)."""
 
-    def __init__(self, surrogate):
+    def __init__(self, surrogate, propose_steps=True):
         self.surrogate = surrogate
+        self.propose_steps = propose_steps
         self.calls = 0
+        self.steps_proposed = 0
 
     def __call__(self, interface, x0, mu0, dx, dmu, ds):
-        if self.surrogate.scales is None:
+        net = self.surrogate
+        if net.scales is None:
             return None
         self.calls += 1
-        xp = self.surrogate.predict(x0.data, dx.data, mu0, ds, (interface.nx, interface.ny, interface.nz))
+        dims = (interface.nx, interface.ny, interface.nz)
+        xp = net.predict(x0.data, dx.data, mu0, ds, dims)
+        if self.propose_steps and net.step_model is not None:
+            corr = float((xp - x0.data - ds * dx.data).pow(2).mean().sqrt())
+            ds_new = net.propose_step(x0.data, dx.data, ds, corr)
+            if abs(ds_new / ds - 1.0) > 0.05:
+                self.steps_proposed += 1
+                xp = net.predict(x0.data, dx.data, mu0, ds_new, dims)
+                return DeviceVector(xp), mu0 + ds_new * dmu, ds_new
         return DeviceVector(xp), mu0 + ds * dmu
