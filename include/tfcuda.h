@@ -372,25 +372,6 @@ int tf_nd_flow_tasks_host(int nnodes, const int32_t *n_own, const int32_t *f, co
                           int nlevels, const int32_t *level_ptr, int fuse_tiles, int chunk_tiles,
                           int32_t *tasks, int32_t *nodes, int max_tasks, int *ntasks);
 
-/* The same application as tf_nd_solve_inv_* in ONE cooperative launch: the
- * products of each tree height and sweep are phases separated by grid-wide
- * barriers (bounded waits); with 0 < top_heights < nlevels only the
- * top_heights heights nearest the root, the others keep their per-height
- * launches around it.  d_work: tf_nd_sweep_workspace_bytes(plan) bytes
- * (0 on a bad plan; a synchronising query), zero-filled before its first use
- * and passed with its size; one
- * application at a time per workspace.  tf_nd_sweep_status returns and
- * clears the sticky error word (TF_ERR_TIMEOUT when a barrier wait gave up),
- * a synchronising read.  No counterpart in the reference.                   */
-size_t tf_nd_sweep_workspace_bytes(const tf_nd_plan *plan);
-int tf_nd_solve_sweep_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_t *d_piv,
-                          double *d_x, void *d_work, size_t work_bytes, int top_heights,
-                          tf_stream_t stream);
-int tf_nd_solve_sweep_f32(const tf_nd_plan *plan, const float *d_fronts, const int32_t *d_piv,
-                          double *d_x, void *d_work, size_t work_bytes, int top_heights,
-                          tf_stream_t stream);
-int tf_nd_sweep_status(void *d_work);
-
 /* ---- learned continuation predictor ---------------------------------------
  * A stack of 3x3x3 convolutions over the cell grid proposing the correction
  * to the secant predictor (x0 + ds*t) of pseudo-arclength continuation; the

@@ -118,30 +118,26 @@ def test_one_application_of_the_inverted_factors_solves(shape, params):
                                                         'Prandtl Number': 2.25, 'X-max': 5,
                                                         'Temperature Forcing': 1.0})])
 def test_dataflow_application_matches_per_height_launches(shape, params, precision):
-    """The one-launch applications of the inverted factors (dataflow over the
-    tree, and cooperative with grid barriers, for every height or for the
-    heights nearest the root only) give the per-height
-    application's result (up to the order of the sums) -- the dataflow one for
-    every split of the fronts into tasks: all split into single strips, the
-    defaults, all fused -- and their bounded waits report no time-out."""
+    """The one-launch dataflow application of the inverted factors (tasks over
+    the tree) gives the per-height application's result (up to the order of
+    the sums) for every split of the fronts into tasks -- all split into
+    single strips, the defaults, all fused -- and its bounded waits report no
+    time-out."""
     import torch
     from transiflow_gb300 import Interface
     nx, ny, nz = shape
     b = None
     results = {}
-    for flow, fuse, chunk in [(False, 48, 24), (True, 0, 1), (True, 0, 24), (True, 48, 24), (True, 10 ** 6, 24),
-                              ('sweep', 0, 0), ('sweep', 2, 0), ('sweep', 4, 0)]:
+    for flow, fuse, chunk in [(False, 48, 24), (True, 0, 1), (True, 0, 24), (True, 48, 24), (True, 10 ** 6, 24)]:
         p = dict(params)
-        p['CUDA'] = {'Factor Precision': precision, 'CUDA Graphs': False, 'Dataflow Apply': flow is True,
-                     'Sweep Apply': (fuse or True) if flow == 'sweep' else False,
+        p['CUDA'] = {'Factor Precision': precision, 'CUDA Graphs': False, 'Dataflow Apply': flow,
                      'Dataflow Fuse Tiles': fuse, 'Dataflow Chunk Tiles': chunk}
         itf = Interface(p, nx, ny, nz)
         st = 0.3 * np.random.default_rng(4).standard_normal(itf.n)
         J = itf.jacobian(itf.vector_from_array(st))
         fac = itf.solver.factorization(J)
         eng = itf.solver._engine(precision)
-        assert (eng.flow is not None) == (flow is True)
-        assert (eng.sweep is not None) == (flow == 'sweep')
+        assert (eng.flow is not None) == flow
         if b is None:
             b = np.random.default_rng(5).standard_normal(itf.n)
             b[itf.dim] = 0.0
@@ -163,26 +159,6 @@ def test_dataflow_application_matches_per_height_launches(shape, params, precisi
         for key, r in results.items():
             assert np.all(np.isfinite(r)), key
             assert np.linalg.norm(r - ref) / np.linalg.norm(ref) <= 3 * err_base + 1e-6, key
-
-
-@pytest.mark.parametrize('precision', ['fp64', 'fp32'])
-def test_sweep_application_in_graphed_gmres(precision):
-    """The cooperative one-launch application inside captured CUDA graphs
-    (the FGMRES Arnoldi steps replay it) solves the gauged system."""
-    from transiflow_gb300 import Interface
-    p = {'Reynolds Number': 1000, 'CUDA': {'Factor Precision': precision, 'Tolerance': 1e-12,
-                                           'Sweep Apply': True}}
-    itf = Interface(p, 40, 40)
-    rng = np.random.default_rng(7)
-    J = itf.jacobian(itf.vector_from_array(0.3 * rng.standard_normal(itf.n)))
-    b = rng.standard_normal(itf.n)
-    for _ in range(3):           # eager, capture, replay
-        y = itf.solve(J, itf.vector_from_array(b)).numpy()
-    A = _gauged(J.to_scipy(), itf.dim)
-    bg = b.copy()
-    bg[itf.dim] = 0
-    assert np.linalg.norm(A @ y - bg) / np.linalg.norm(bg) < 1e-11
-    assert itf.solver._engine(precision).sweep is not None
 
 
 def test_dataflow_wait_times_out_and_reports():

@@ -24,7 +24,7 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 SOURCES = [('tf_assemble.cu', ['-fmad=false']), ('tf_sparse.cu', []), ('tf_nd.cu', []), ('tf_nd_panel_f32.cu', []),
            ('tf_nd_panel_f64.cu', []),
            ('tf_nd_inv.cu', []), ('tf_nd_tc.cu', []), ('tf_nd_flow.cu', []),
-           ('tf_nd_sweep.cu', []), ('tf_surrogate.cu', [])]
+           ('tf_surrogate.cu', [])]
 
 TF_MAX_BC_OPS = 24
 TF_METRIC_FIELDS = 10
@@ -149,10 +149,6 @@ _SIGNATURES = {
     'tf_nd_solve_flow_f32': ([_P, _P, _P, _P, _P, _P], _I),
     'tf_nd_flow_status': ([_P], _I),
     'tf_nd_flow_tasks_host': ([_I, _P, _P, _P, _I, _P, _I, _I, _P, _P, _I, _P], _I),
-    'tf_nd_sweep_workspace_bytes': ([_P], ctypes.c_size_t),
-    'tf_nd_solve_sweep_f64': ([_P, _P, _P, _P, _P, ctypes.c_size_t, _I, _P], _I),
-    'tf_nd_solve_sweep_f32': ([_P, _P, _P, _P, _P, ctypes.c_size_t, _I, _P], _I),
-    'tf_nd_sweep_status': ([_P], _I),
     'tf_sg_conv': ([_I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _I, _P], _I),
     'tf_sg_wgrad_workspace_bytes': ([_I, _I, _I], ctypes.c_size_t),
     'tf_sg_wgrad': ([_I, _I, _I, _I, _I, _P, _P, _P, _I, _P, ctypes.c_size_t, _P], _I),

@@ -35,11 +35,6 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       for the fronts it depends on (default False; plans whose
                       widest front does not fit that launch's shared memory
                       keep one launch per tree height)
-  'Sweep Apply'       with 'Inverse Apply': both sweeps in one cooperative
-                      launch, the tree heights separated by grid-wide barriers
-                      (True), or only the k heights nearest the root (an int
-                      k), the others keeping their per-height launches
-                      (default False)
   'Dataflow Fuse Tiles', 'Dataflow Chunk Tiles'
                       fronts with at most this many 32x32 factor tiles per
                       sweep run as one task (default 48); target tiles per task
@@ -227,7 +222,6 @@ class Interface(_Base):
                              flow_fuse_tiles=int(opts.get('Dataflow Fuse Tiles', 48)),
                              flow_chunk_tiles=int(opts.get('Dataflow Chunk Tiles', 24)),
                              leaf_cells=int(opts.get('Leaf Cells', 48)),
-                             sweep=opts.get('Sweep Apply', False),
                              tc_min_front=(int(opts.get('Tensor Core Min Front', 1024))
                                            if opts.get('Tensor Cores', True) else 0),
                              tc_terms=1 if opts.get('Tensor Core Precision', 'tf32x3') == 'tf32' else 3,

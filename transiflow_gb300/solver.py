@@ -226,7 +226,7 @@ class _Engine:
         # FP32 factors may be applied from a BF16 copy (half the bytes)
         self.bf16 = None
         if not f64 and solver.storage == 'bf16':
-            if not solver.inverse or solver.flow or solver.sweep:
+            if not solver.inverse or solver.flow:
                 raise ValueError("BF16 factor storage needs 'Inverse Apply' with the per-height application")
             self.bf16 = torch.empty(plan.front_elems, dtype=torch.bfloat16, device=dev)
         if solver.inverse:
@@ -237,15 +237,7 @@ class _Engine:
             wbytes = lib.tf_nd_invert_workspace_bytes(sp, 8 if f64 else 4)
             self.work = torch.empty(max(1, (wbytes + 7) // 8), dtype=torch.float64, device=dev)
             self.flow = None
-            self.sweep = None
-            if solver.sweep:
-                # both sweeps in one cooperative launch, heights separated by
-                # grid barriers
-                sw_bytes = lib.tf_nd_sweep_workspace_bytes(sp)
-                # zero-filled: its first word is the sticky error word
-                self.sweep = torch.zeros((sw_bytes + 7) // 8, dtype=torch.float64, device=dev)
-                sweep_fn = lib.tf_nd_solve_sweep_f64 if f64 else lib.tf_nd_solve_sweep_f32
-            elif solver.flow:
+            if solver.flow:
                 # both sweeps in one persistent launch (dataflow over the
                 # elimination tree); plans whose widest front does not fit
                 # the launch's shared memory keep the per-height launches
@@ -258,13 +250,7 @@ class _Engine:
                         self.flow = flow
                     elif code != 4:     # TF_ERR_SIZE: fall back to the per-height launches
                         _lib.check(code, 'tf_nd_flow_prepare')
-            if self.sweep is not None:
-
-                def solve():
-                    _lib.check(sweep_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(),
-                                        self.sweep.data_ptr(), self.sweep.numel() * 8, solver.sweep_heights,
-                                        _stream()), 'tf_nd_solve_sweep')
-            elif self.flow is not None:
+            if self.flow is not None:
                 flow_fn = lib.tf_nd_solve_flow_f64 if f64 else lib.tf_nd_solve_flow_f32
 
                 def solve():
@@ -300,7 +286,6 @@ class _Engine:
                                'tf_nd_factors_to_bf16')
         else:
             self.flow = None
-            self.sweep = None
             sol_fn = lib.tf_nd_solve_f64 if f64 else lib.tf_nd_solve_f32
 
             def factor():
@@ -325,8 +310,6 @@ class _Engine:
         since the last check (synchronising)."""
         if self.flow is not None:
             _lib.check(self.lib.tf_nd_flow_status(self.flow.data_ptr()), 'tf_nd_solve_flow')
-        if self.sweep is not None:
-            _lib.check(self.lib.tf_nd_sweep_status(self.sweep.data_ptr()), 'tf_nd_solve_sweep')
 
 
 def _struct_ptr(s):
@@ -339,7 +322,7 @@ class Solver:
 
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
                  reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True, flow=False,
-                 flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48, sweep=False, tc_min_front=1024,
+                 flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48, tc_min_front=1024,
                  tc_terms=3, storage='fp32', inner='fp64'):
         self.itf = interface
         # FP32 factorisations: heights whose widest front has at least this
@@ -362,11 +345,6 @@ class Solver:
         self.inverse = inverse
         # dataflow application (one launch for both sweeps) of the inverted factors
         self.flow = flow and inverse
-        # cooperative one-launch application, heights separated by grid
-        # barriers: True for every height, an int k for the k heights nearest
-        # the root (the others keep their per-height launches)
-        self.sweep = bool(sweep) and inverse
-        self.sweep_heights = 0 if sweep is True else int(sweep or 0)
         self.flow_fuse_tiles = flow_fuse_tiles
         self.flow_chunk_tiles = flow_chunk_tiles
         self.graphs = graphs
