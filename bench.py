@@ -236,6 +236,7 @@ def train_predictor(args):
     t0 = time.perf_counter()
     groups = []
     stalls = []
+    dropped = 0
     for n in [int(v) for v in args.train_grids.split(',')]:
         for seed in [int(v) for v in args.train_seeds.split(',')]:
             itf = Interface({'CUDA': solver_options(args, 'fp32')}, n, n, n)
@@ -260,7 +261,11 @@ def train_predictor(args):
                 if 'stalled' not in str(e):
                     raise
                 stalls.append((n, seed, float(itf.get_parameter('Reynolds Number'))))
-            groups.append(((n, n, n), rec.samples))
+            # regular steps only: near a singular point the accepted steps
+            # shrink to ~0.01 and (x1 - secant) / ds^2 explodes
+            kept = [smp for smp in rec.samples if smp['ds'] >= 0.25 * args.train_ds and (smp['its'] or 0) >= 1]
+            dropped += len(rec.samples) - len(kept)
+            groups.append(((n, n, n), kept))
             del itf, cont, x0
             _free()
     branches_s = time.perf_counter() - t0
@@ -278,7 +283,7 @@ def train_predictor(args):
     torch.cuda.synchronize()
     info = {'branches': len(groups), 'points': sum(len(g) for _, g in groups), 'branches_s': branches_s,
             'step_model': step_model,
-            'ended_at_singular_point': stalls,
+            'ended_at_singular_point': stalls, 'irregular_points_dropped': dropped,
             'train_s': time.perf_counter() - t1, 'adam_steps': args.train_rounds * args.train_steps * len(groups),
             'final_loss': losses[-1] if losses else None, 'parameters': net.parameters()}
     return net, info

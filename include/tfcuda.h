@@ -186,6 +186,16 @@ int tf_spmv_f32(int n, const int32_t *d_rowptr, const int32_t *d_cols,
                 const float *d_vals, const double *d_x, double *d_y,
                 double alpha, double beta, tf_stream_t stream);
 
+/* Equilibration before a low-precision factorisation (no counterpart in the
+ * reference, whose SuperLU factors in FP64): row scales d_rscale[i] and
+ * column scales d_cscale[j], powers of two near 1 / max |entry| of the row
+ * and then of the row-scaled column (1 for empty ones), and d_out[k] =
+ * d_rscale[row] * d_vals[k] * d_cscale[col] (d_out may alias d_vals).  The
+ * preconditioner of A is then d_cscale .* (LU of d_out)^-1 (d_rscale .* b).  */
+int tf_equilibrate(int n, const int32_t *d_rowptr, const int32_t *d_cols, const double *d_vals,
+                   double *d_rscale, double *d_cscale, double *d_out, tf_stream_t stream);
+/* y[i] = d[i] * x[i] (y may alias x).                                         */
+int tf_vec_mul(int n, const double *d_d, const double *d_x, double *d_y, tf_stream_t stream);
 /* y[i] += a * diag[i] * x[i] (diagonal matrix product used by theta-method
  * residuals and J - M / (theta dt)).                                         */
 int tf_diag_axpy(int n, double a, const double *d_diag, const double *d_x, double *d_y,

@@ -117,6 +117,8 @@ _SIGNATURES = {
     'tf_gauge_values': ([_I, _P, _P, _P, _I, _P, _P], _I),
     'tf_spmv_f64': ([_I, _P, _P, _P, _P, _P, _D, _D, _P], _I),
     'tf_nd_tc_update_f32': ([_P, _I, _I, _I, _P, _P, _P], _I),
+    'tf_equilibrate': ([_I, _P, _P, _P, _P, _P, _P, _P], _I),
+    'tf_vec_mul': ([_I, _P, _P, _P, _P], _I),
     'tf_spmv_f32': ([_I, _P, _P, _P, _P, _P, _D, _D, _P], _I),
     'tf_diag_axpy': ([_I, _D, _P, _P, _P, _P], _I),
     'tf_add_diagonal': ([_I, _P, _P, _P, _D, _P, _P], _I),

@@ -489,18 +489,19 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node
     }
 }
 
-// The boundary products with BF16-stored factors, products and sums in FP32.
-// cp.async has no 2-byte form and rows start at any 2-byte alignment, so a
-// warp loads each 32 x 32 tile with plain loads (a 64-byte segment per row,
-// all 32 rows in flight), widens it to FP32 in shared memory and forms one
-// row's dot product per lane; the next tile's loads are issued before the
-// current tile's products.
-template <bool FWD>
-__global__ void __launch_bounds__(BV_THREADS) inv_bnd_bf16_kernel(DevPlan P, int node0, int ctiles,
-                                                                  const __nv_bfloat16 *fronts, double *x,
-                                                                  double *packed) {
-    __shared__ float tiles[BV_WARPS][TILE];
-    __shared__ float v[BV_TILES * SB];
+// The boundary products for FP32 and BF16 factors, FP32 arithmetic.  A warp
+// owns 32 rows and up to ctiles 32-column tiles of one front; for every row
+// its lanes load 32 consecutive columns (one coalesced 128-byte or 64-byte
+// segment), multiply them by the vector entry each lane holds for its
+// column and accumulate per row, so each lane ends with 32 partial sums
+// (one per row); a butterfly of 31 shuffles then leaves lane l with row l's
+// total.  One load instruction per 32 factor entries, against one cp.async
+// per entry in the tile kernel above (whose serial per-lane dot products
+// avoid FP64 shuffles).  The first tile's loads are issued before the wait
+// for the previous launch.
+template <typename S, bool FWD>
+__global__ void __launch_bounds__(BV_THREADS) inv_bnd_rows_kernel(DevPlan P, int node0, int ctiles, const S *fronts,
+                                                                  double *x, double *packed) {
     pdl_trigger();
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
@@ -511,50 +512,59 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_bf16_kernel(DevPlan P, int
     const int cbase = clo + blockIdx.z * ccols;
     if (rbase >= rhi || cbase >= chi) return;
     const int cend = min(chi, cbase + ccols);
-    const __nv_bfloat16 *F = fronts + P.front_off[node];
+    const S *F = fronts + P.front_off[node];
     const int32_t *g = P.idx + P.idx_off[node];
     double *pk = packed + P.idx_off[node];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int r0 = rbase + warp * SB;
-    float *buf = tiles[warp];
-    // the first tile of the factors in registers before the wait
-    float nxt[SB];
-    auto fetch = [&](int c0) {
-        const bool colok = c0 + lane < cend;
+    const int nrows = min(SB, rhi - r0);       // may be <= 0 for the second warp
+    float acc[SB];
+    {
+        // first tile, before the wait (the factors do not change)
+        const int c = cbase + lane;
+        const bool cok = c < cend;
 #pragma unroll
-        for (int i = 0; i < SB; ++i) {
-            const int r = r0 + i;
-            nxt[i] = (colok && r < rhi) ? __bfloat162float(F[(size_t)r * f + c0 + lane]) : 0.f;
-        }
-    };
-    if (r0 < rhi) fetch(cbase);
-    constexpr int PER = BV_TILES * SB / BV_THREADS;
-    int32_t vi[PER];
+        for (int i = 0; i < SB; ++i) acc[i] = (cok && i < nrows) ? widen(F[(size_t)(r0 + i) * f + c]) : 0.f;
+    }
+    int32_t vi[BV_TILES];
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        const int c = threadIdx.x + q * BV_THREADS;
-        vi[q] = (c < ccols && cbase + c < cend) ? (FWD ? cbase + c : g[cbase + c]) : -1;
+    for (int t = 0; t < BV_TILES; ++t) {
+        const int c = cbase + t * SB + lane;
+        vi[t] = (t < ctiles && c < cend) ? (FWD ? c : g[c]) : -1;
     }
     pdl_wait();
+    if (nrows <= 0) return;
+    float v[BV_TILES];
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        const int c = threadIdx.x + q * BV_THREADS;
-        if (c < ccols) v[c] = vi[q] >= 0 ? (float)(FWD ? pk[vi[q]] : x[vi[q]]) : 0.f;
-    }
-    __syncthreads();
-    if (r0 >= rhi) return;
-    float s = 0.f;
-    for (int c0 = cbase; c0 < cend; c0 += SB) {
+    for (int t = 0; t < BV_TILES; ++t) v[t] = vi[t] >= 0 ? (float)(FWD ? pk[vi[t]] : x[vi[t]]) : 0.f;
 #pragma unroll
-        for (int i = 0; i < SB; ++i) buf[i * TSTRIDE + lane] = nxt[i];
-        __syncwarp();
-        if (c0 + SB < cend) fetch(c0 + SB);
-        s += tile_dot_n(buf, v + (c0 - cbase), lane, cend - c0);
-        __syncwarp();
+    for (int i = 0; i < SB; ++i) acc[i] *= v[0];
+#pragma unroll
+    for (int t = 1; t < BV_TILES; ++t) {
+        if (t >= ctiles || cbase + t * SB >= cend) break;
+        const int c = cbase + t * SB + lane;
+        const bool cok = c < cend;
+        float ld[SB];
+#pragma unroll
+        for (int i = 0; i < SB; ++i) ld[i] = (cok && i < nrows) ? widen(F[(size_t)(r0 + i) * f + c]) : 0.f;
+#pragma unroll
+        for (int i = 0; i < SB; ++i) acc[i] = fmaf(ld[i], v[t], acc[i]);
     }
-    if (r0 + lane < rhi) {
-        if (FWD) atomicAdd(x + g[r0 + lane], -(double)s);
-        else atomicAdd(pk + r0 + lane, -(double)s);
+    // transpose-reduce: after the step with offset o a lane keeps o sums, the
+    // half of its rows selected by its lane bit o
+#pragma unroll
+    for (int o = SB / 2; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < o; ++i) {
+            const float send = upper ? acc[i] : acc[i + o];
+            const float keep = upper ? acc[i + o] : acc[i];
+            acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    if (lane < nrows) {
+        if (FWD) atomicAdd(x + g[r0 + lane], -(double)acc[0]);
+        else atomicAdd(pk + r0 + lane, -(double)acc[0]);
     }
 }
 
@@ -615,8 +625,8 @@ static int inv_bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, int
     const int ctiles = wide >= 4 * nsm ? BV_TILES : 1;
     dim3 grid(rb, cnt, (cols + ctiles * SB - 1) / (ctiles * SB));
     cudaError_t ce;
-    if constexpr (sizeof(T) == 2)
-        ce = launch_pdl(pdl, inv_bnd_bf16_kernel<FWD>, grid, dim3(BV_THREADS), 0, s, D, node0, ctiles, fronts, x,
+    if constexpr (sizeof(T) <= 4)
+        ce = launch_pdl(pdl, inv_bnd_rows_kernel<T, FWD>, grid, dim3(BV_THREADS), 0, s, D, node0, ctiles, fronts, x,
                         packed);
     else
         ce = launch_pdl(pdl, inv_bnd_kernel<T, FWD>, grid, dim3(BV_THREADS), sizeof(T) * 2 * BV_WARPS * TILE, s, D,

@@ -311,6 +311,84 @@ extern "C" int tf_spmv_f32(int n, const int32_t *d_rowptr, const int32_t *d_cols
     return cuda_status();
 }
 
+// ---------------------------------------------------------------------------
+// Equilibration of an operator before a low-precision factorisation: row
+// scales d_r = 2^-e (max_j |a_ij| = f 2^e, 1/2 <= f < 1), then column scales
+// d_c of the row-scaled matrix the same way, and the scaled values
+// d_r[i] a_ij d_c[j].  Powers of two: the scaling itself is exact in FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double pow2_recip(double m) {
+    int e = 0;
+    frexp(m, &e);
+    return ldexp(1.0, -e);
+}
+
+__global__ void eq_rows_kernel(int n, const int32_t *__restrict__ rowptr, const double *__restrict__ vals,
+                               double *__restrict__ dr, unsigned long long *__restrict__ cbits) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double m = 0.0;
+    for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) m = fmax(m, fabs(vals[k]));
+    dr[r] = m > 0.0 ? pow2_recip(m) : 1.0;
+    cbits[r] = 0ull;
+}
+
+// column maxima of the row-scaled values: non-negative doubles order like
+// their bit patterns, so an integer atomicMax on the bits is a maximum
+__global__ void eq_cols_kernel(int n, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
+                               const double *__restrict__ vals, const double *__restrict__ dr,
+                               unsigned long long *__restrict__ cbits) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const double s = dr[r];
+    for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+        const double a = fabs(vals[k] * s);
+        if (a > 0.0) atomicMax(cbits + cols[k], (unsigned long long)__double_as_longlong(a));
+    }
+}
+
+__global__ void eq_finish_kernel(int n, unsigned long long *__restrict__ cbits) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double m = __longlong_as_double((long long)cbits[j]);
+    reinterpret_cast<double *>(cbits)[j] = m > 0.0 ? pow2_recip(m) : 1.0;
+}
+
+__global__ void eq_scale_kernel(int n, const int32_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
+                                const double *vals, const double *__restrict__ dr, const double *__restrict__ dc,
+                                double *out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const double s = dr[r];
+    for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) out[k] = vals[k] * s * dc[cols[k]];
+}
+
+__global__ void vec_mul_kernel(int n, const double *__restrict__ d, const double *x, double *y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = d[i] * x[i];
+}
+
+extern "C" int tf_equilibrate(int n, const int32_t *d_rowptr, const int32_t *d_cols, const double *d_vals,
+                              double *d_rscale, double *d_cscale, double *d_out, tf_stream_t stream) {
+    if (n <= 0 || !d_rowptr || !d_cols || !d_vals || !d_rscale || !d_cscale || !d_out) return TF_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    auto *cbits = reinterpret_cast<unsigned long long *>(d_cscale);
+    const int b = blocks_for(n, 256);
+    eq_rows_kernel<<<b, 256, 0, s>>>(n, d_rowptr, d_vals, d_rscale, cbits);
+    eq_cols_kernel<<<b, 256, 0, s>>>(n, d_rowptr, d_cols, d_vals, d_rscale, cbits);
+    eq_finish_kernel<<<b, 256, 0, s>>>(n, cbits);
+    eq_scale_kernel<<<b, 256, 0, s>>>(n, d_rowptr, d_cols, d_vals, d_rscale, d_cscale, d_out);
+    launched(4);
+    return cuda_status();
+}
+
+extern "C" int tf_vec_mul(int n, const double *d_d, const double *d_x, double *d_y, tf_stream_t stream) {
+    if (n <= 0 || !d_d || !d_x || !d_y) return TF_ERR_ARG;
+    vec_mul_kernel<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, d_d, d_x, d_y);
+    launched();
+    return cuda_status();
+}
+
 extern "C" int tf_diag_axpy(int n, double a, const double *d_diag, const double *d_x, double *d_y,
                             tf_stream_t stream) {
     if (n <= 0 || !d_diag || !d_x || !d_y) return TF_ERR_ARG;

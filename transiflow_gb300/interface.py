@@ -50,6 +50,10 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       factorisation the entries the preconditioner reads are
                       rounded to a BF16 copy, and every application reads
                       that copy (half the bytes) with FP32 products and sums
+  'Equilibrate'       FP32 factors: factor the operator scaled by powers of two
+                      per row and column (1 / the largest entry), so that the
+                      FP32 rounding does not wipe out badly scaled equations
+                      (default True; FP64 factors are never scaled)
   'Inner Precision'   'fp64' (default) or 'fp32': the Arnoldi products of
                       FGMRES use an FP32 copy of the gauged Jacobian (SpMV in
                       FP32 values, FP64 vectors); every restart cycle stops
@@ -226,7 +230,8 @@ class Interface(_Base):
                                            if opts.get('Tensor Cores', True) else 0),
                              tc_terms=1 if opts.get('Tensor Core Precision', 'tf32x3') == 'tf32' else 3,
                              storage=opts.get('Factor Storage', 'fp32'),
-                             inner=opts.get('Inner Precision', 'fp64'))
+                             inner=opts.get('Inner Precision', 'fp64'),
+                             equilibrate=opts.get('Equilibrate', True))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

@@ -223,6 +223,17 @@ class _Engine:
         self.struct.tc_terms = solver.tc_terms
         sp = _struct_ptr(self.struct)
         dev = solver.itf.device
+        # FP32 factors of an equilibrated copy of the operator: powers-of-two
+        # row and column scales keep the FP32 factorisation of badly scaled
+        # Jacobians (Pr = 1000 convection) useful; the staging buffer keeps
+        # the unscaled values (the reuse policy measures drift on them)
+        self.equil = (not f64) and solver.equilibrate
+        n = plan.host.n
+        if self.equil:
+            self.scaled = torch.empty_like(self.staging)
+            self.rscale = torch.empty(n, dtype=torch.float64, device=dev)
+            self.cscale = torch.empty(n, dtype=torch.float64, device=dev)
+        src = self.scaled if self.equil else self.staging
         # FP32 factors may be applied from a BF16 copy (half the bytes)
         self.bf16 = None
         if not f64 and solver.storage == 'bf16':
@@ -278,7 +289,7 @@ class _Engine:
             facinv_fn = lib.tf_nd_factor_inv_f64 if f64 else lib.tf_nd_factor_inv_f32
 
             def factor():
-                _lib.check(facinv_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
+                _lib.check(facinv_fn(sp, src.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
                                      info.data_ptr(), self.work.data_ptr(), wbytes, _stream(),
                                      ctypes.c_void_p(self.aux.cuda_stream)), 'tf_nd_factor_inv')
                 if self.bf16 is not None:
@@ -289,12 +300,30 @@ class _Engine:
             sol_fn = lib.tf_nd_solve_f64 if f64 else lib.tf_nd_solve_f32
 
             def factor():
-                _lib.check(fac_fn(sp, self.staging.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
+                _lib.check(fac_fn(sp, src.data_ptr(), fronts.data_ptr(), piv.data_ptr(),
                                   info.data_ptr(), _stream()), 'tf_nd_factor')
 
             def solve():
                 _lib.check(sol_fn(sp, fronts.data_ptr(), piv.data_ptr(), self.vec.data_ptr(), _stream()),
                            'tf_nd_solve')
+
+        if self.equil:
+            pat = solver.itf.pattern
+            factor_scaled, solve_scaled = factor, solve
+
+            def factor():
+                _lib.check(lib.tf_equilibrate(n, pat.rowptr.data_ptr(), pat.cols.data_ptr(), self.staging.data_ptr(),
+                                              self.rscale.data_ptr(), self.cscale.data_ptr(), self.scaled.data_ptr(),
+                                              _stream()), 'tf_equilibrate')
+                factor_scaled()
+
+            def solve():
+                # M^-1 b = D_c (LU of D_r A D_c)^-1 (D_r b)
+                _lib.check(lib.tf_vec_mul(n, self.rscale.data_ptr(), self.vec.data_ptr(), self.vec.data_ptr(),
+                                          _stream()), 'tf_vec_mul')
+                solve_scaled()
+                _lib.check(lib.tf_vec_mul(n, self.cscale.data_ptr(), self.vec.data_ptr(), self.vec.data_ptr(),
+                                          _stream()), 'tf_vec_mul')
 
         self.solve_raw = solve
         self.lib = lib
@@ -323,7 +352,7 @@ class Solver:
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
                  reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True, flow=False,
                  flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48, tc_min_front=1024,
-                 tc_terms=3, storage='fp32', inner='fp64'):
+                 tc_terms=3, storage='fp32', inner='fp64', equilibrate=True):
         self.itf = interface
         # FP32 factorisations: heights whose widest front has at least this
         # many rows use blocked rank-256 tensor-core updates (0: never)
@@ -340,6 +369,8 @@ class Solver:
             raise ValueError("'Inner Precision' must be 'fp64' or 'fp32'")
         self.inner = inner
         self._opbuf32 = None
+        # FP32 factors: factor the row- and column-equilibrated operator
+        self.equilibrate = bool(equilibrate)
         # grid cells at which nested dissection stops splitting a box
         self.leaf_cells = leaf_cells
         self.inverse = inverse

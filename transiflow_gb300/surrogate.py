@@ -372,7 +372,9 @@ class LearnedPredictor:
     step size: the network's predicted correction of the secant predictor
     gives the branch's curvature, from which ``Surrogate.propose_step``
     picks the step (the network then predicts again at that step).  The
-    reference picks steps by Newton counts only (Continuation.py:197-209)."""
+    reference picks steps by Newton counts only (Continuation.py:197-209).
+    A network whose calibrated error is not below the secant predictor's
+    (eps >= 1) proposes nothing, and steps are proposed only for eps < 1/2."""
 
     def __init__(self, surrogate, propose_steps=True):
         self.surrogate = surrogate
@@ -380,14 +382,22 @@ class LearnedPredictor:
         self.calls = 0
         self.steps_proposed = 0
 
+    # a calibrated network no better than the secant predictor is not used;
+    # steps are proposed only by one clearly better
+    USE_BELOW = 1.0
+    PROPOSE_BELOW = 0.5
+
     def __call__(self, interface, x0, mu0, dx, dmu, ds):
         net = self.surrogate
         if net.scales is None:
             return None
+        sm = net.step_model
+        if sm is not None and not sm['eps'] < self.USE_BELOW:
+            return None
         self.calls += 1
         dims = (interface.nx, interface.ny, interface.nz)
         xp = net.predict(x0.data, dx.data, mu0, ds, dims)
-        if self.propose_steps and net.step_model is not None:
+        if self.propose_steps and sm is not None and sm['eps'] < self.PROPOSE_BELOW:
             corr = float((xp - x0.data - ds * dx.data).pow(2).mean().sqrt())
             ds_new = net.propose_step(x0.data, dx.data, ds, corr)
             if abs(ds_new / ds - 1.0) > 0.05:
