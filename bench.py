@@ -263,12 +263,25 @@ def train_predictor(args):
                 stalls.append((n, seed, float(itf.get_parameter('Reynolds Number'))))
             # regular steps only: near a singular point the accepted steps
             # shrink to ~0.01 and (x1 - secant) / ds^2 explodes
-            kept = [smp for smp in rec.samples if smp['ds'] >= 0.25 * args.train_ds and (smp['its'] or 0) >= 1]
+            # and not the first step from Re = 0, whose correction is not of
+            # order ds^2 (the reference's Re = 0 -> 1 viscosity substitution)
+            kept = [smp for smp in rec.samples if smp['ds'] >= 0.25 * args.train_ds and (smp['its'] or 0) >= 1
+                    and smp['mu'] > 0.0]
             dropped += len(rec.samples) - len(kept)
             groups.append(((n, n, n), kept))
             del itf, cont, x0
             _free()
     branches_s = time.perf_counter() - t0
+    # robust to the remaining outliers: drop samples whose scaled correction
+    # (x1 - secant) / ds^2 is more than ten times the median's
+    size = {id(smp): float((smp['x1'] - smp['x0'] - smp['ds'] * smp['t']).pow(2).mean().sqrt()) / smp['ds'] ** 2
+            for _, g in groups for smp in g}
+    med = float(np.median(list(size.values()))) if size else 0.0
+    outliers = 0
+    for k, (dims, g) in enumerate(groups):
+        keep = [smp for smp in g if size[id(smp)] <= 10.0 * med]
+        outliers += len(g) - len(keep)
+        groups[k] = (dims, keep)
     net = Surrogate(4)
     net.fit_scales([smp for _, g in groups for smp in g])
     t1 = time.perf_counter()
@@ -284,6 +297,7 @@ def train_predictor(args):
     info = {'branches': len(groups), 'points': sum(len(g) for _, g in groups), 'branches_s': branches_s,
             'step_model': step_model,
             'ended_at_singular_point': stalls, 'irregular_points_dropped': dropped,
+            'outliers_dropped': outliers,
             'train_s': time.perf_counter() - t1, 'adam_steps': args.train_rounds * args.train_steps * len(groups),
             'final_loss': losses[-1] if losses else None, 'parameters': net.parameters()}
     return net, info
