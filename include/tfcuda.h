@@ -405,7 +405,8 @@ int tf_nd_flow_tasks_host(int nnodes, const int32_t *n_own, const int32_t *f, co
  *   tf_sg_loss_workspace_bytes.
  * tf_sg_act_grad: dZ = dA where Z > 0 else 0, FP32 and BF16 (n elements).
  * tf_sg_pack: the network input from the FP64 state x and tangent t (scaled
- *   by the host arrays sx, st of dof entries), the parameter mu and step ds.
+ *   by the host arrays sx, st of dof entries), optionally a third field p
+ *   (d_p, scaled by sp; NULL: none), then the parameter mu and step ds.
  * tf_sg_target: tgt = (x1 - x0 - ds t) * inv_scale[d] (FP32).
  * tf_sg_unpack: xp = x0 + ds t + scale[d] * out[cell][d] (FP64); entries
  *   whose tangent t is exactly zero (unknowns the branch does not move, such
@@ -423,8 +424,9 @@ int tf_sg_loss(int ncell, int dof, int np, const float *d_out, const float *d_tg
                double *d_loss, void *d_work, size_t work_bytes, tf_stream_t stream);
 int tf_sg_act_grad(long long n, const float *d_da, const float *d_z, float *d_dzf, void *d_dzh,
                    tf_stream_t stream);
-int tf_sg_pack(int ncell, int dof, int kp, const double *d_x, const double *d_t, const float *sx,
-               const float *st, float mu, float ds, void *d_x0, tf_stream_t stream);
+int tf_sg_pack(int ncell, int dof, int kp, const double *d_x, const double *d_t, const double *d_p,
+               const float *sx, const float *st, const float *sp, float mu, float ds, void *d_x0,
+               tf_stream_t stream);
 int tf_sg_target(int ncell, int dof, const double *d_x0, const double *d_t, const double *d_x1, double ds,
                  const double *inv_scale, float *d_tgt, tf_stream_t stream);
 int tf_sg_unpack(int ncell, int dof, int np, const float *d_out, const double *d_x0, const double *d_t,

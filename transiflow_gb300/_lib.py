@@ -157,7 +157,7 @@ _SIGNATURES = {
     'tf_sg_loss_workspace_bytes': ([_I, _I], ctypes.c_size_t),
     'tf_sg_loss': ([_I, _I, _I, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], _I),
     'tf_sg_act_grad': ([ctypes.c_longlong, _P, _P, _P, _P, _P], _I),
-    'tf_sg_pack': ([_I, _I, _I, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P], _I),
+    'tf_sg_pack': ([_I, _I, _I, _P, _P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P], _I),
     'tf_sg_target': ([_I, _I, _P, _P, _P, _D, _P, _P, _P], _I),
     'tf_sg_unpack': ([_I, _I, _I, _P, _P, _P, _D, _P, _P, _P], _I),
     'tf_sg_adam': ([_I, _I, _P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,

@@ -309,16 +309,19 @@ __global__ void act_grad_kernel(long long n, const float *__restrict__ da, const
 // Network input: state x and tangent t scaled per variable, then the
 // parameter and the step as constant channels, zero padding up to kp.
 __global__ void pack_kernel(int ncell, int dof, int kp, const double *__restrict__ x, const double *__restrict__ t,
-                            FieldScales sc, float mu, float ds, __nv_bfloat16 *__restrict__ X0) {
+                            const double *__restrict__ pv, FieldScales sc, FieldScales sp, float mu, float ds,
+                            __nv_bfloat16 *__restrict__ X0) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)ncell * kp) return;
     const long long c = e / kp;
     const int ch = (int)(e % kp);
+    const int nf = pv ? 3 : 2;          // fields before mu and ds
     float v = 0.f;
     if (ch < dof) v = (float)x[c * dof + ch] * sc.a[ch];
     else if (ch < 2 * dof) v = (float)t[c * dof + ch - dof] * sc.b[ch - dof];
-    else if (ch == 2 * dof) v = mu;
-    else if (ch == 2 * dof + 1) v = ds;
+    else if (pv && ch < 3 * dof) v = (float)pv[c * dof + ch - 2 * dof] * sp.a[ch - 2 * dof];
+    else if (ch == nf * dof) v = mu;
+    else if (ch == nf * dof + 1) v = ds;
     X0[e] = __float2bfloat16(v);
 }
 
@@ -473,18 +476,21 @@ extern "C" int tf_sg_act_grad(long long n, const float *d_da, const float *d_z, 
     return cuda_status();
 }
 
-extern "C" int tf_sg_pack(int ncell, int dof, int kp, const double *d_x, const double *d_t, const float *sx,
-                          const float *st, float mu, float ds, void *d_x0, tf_stream_t stream) {
-    if (ncell <= 0 || dof <= 0 || dof > MAX_DOF || 2 * dof + 2 > kp || !ch_ok(kp) || !d_x || !d_t || !sx || !st ||
-        !d_x0)
+extern "C" int tf_sg_pack(int ncell, int dof, int kp, const double *d_x, const double *d_t, const double *d_p,
+                          const float *sx, const float *st, const float *sp, float mu, float ds, void *d_x0,
+                          tf_stream_t stream) {
+    const int nf = d_p ? 3 : 2;
+    if (ncell <= 0 || dof <= 0 || dof > MAX_DOF || nf * dof + 2 > kp || !ch_ok(kp) || !d_x || !d_t || !sx || !st ||
+        (d_p && !sp) || !d_x0)
         return TF_ERR_ARG;
-    FieldScales sc = {};
+    FieldScales sc = {}, spc = {};
     for (int d = 0; d < dof; ++d) {
         sc.a[d] = sx[d];
         sc.b[d] = st[d];
+        spc.a[d] = d_p ? sp[d] : 0.f;
     }
     pack_kernel<<<blocks((long long)ncell * kp, 256), 256, 0, (cudaStream_t)stream>>>(
-        ncell, dof, kp, d_x, d_t, sc, mu, ds, static_cast<__nv_bfloat16 *>(d_x0));
+        ncell, dof, kp, d_x, d_t, d_p, sc, spc, mu, ds, static_cast<__nv_bfloat16 *>(d_x0));
     launched();
     return cuda_status();
 }

@@ -2,16 +2,21 @@
 branch points that plain continuation computes.
 
 The network reads the current state ``x``, the secant tangent ``t``, the
-parameter ``mu`` and the step ``ds`` on the cell grid and proposes the
-correction to the secant predictor ``x + ds*t``.  The Newton corrector of the
+previous step's correction of the secant predictor per unit step squared
+``p`` (the change of the secant tangent over the last step -- a quadratic
+extrapolation the network refines, since a 3x3x3 stencil network alone sees
+only nine cells of what is a global curvature), the parameter ``mu`` and the
+step ``ds`` on the cell grid and proposes the correction to the secant
+predictor ``x + ds*t``, and through it the next step size.  The Newton corrector of the
 continuation judges every point; the secant predictor is the fallback
 whenever the corrector started from the learned predictor does not converge
 within ``Continuation(learned_newton_iterations=4)`` iterations.
 
 Architecture: ``layers`` 3x3x3 convolutions over the cell grid (a 2D grid is
 a grid one cell thick), ``channels`` channels between them, ReLU after every
-layer but the last.  Inputs are ``2*dof + 2`` channels (x and t per
-variable, mu and ds as constant fields), outputs ``dof`` channels.  Forward,
+layer but the last.  Inputs are ``3*dof + 2`` channels (x, t and p per
+variable, mu and ds as constant fields; ``2*dof + 2`` without p), outputs
+``dof`` channels.  Forward,
 backward and Adam run in libtfcuda kernels (``tf_sg_*``): BF16 operands with
 FP32 accumulation on the tensor cores, FP32 master weights.  Inputs and
 targets are scaled per variable with statistics of the training samples; the
@@ -67,26 +72,49 @@ def check_field(t, n, name='field'):
         raise ValueError('%s has %d values, the grid needs %d' % (name, t.numel(), n))
 
 
+class _History:
+    """The previous step's correction of the secant predictor, per unit
+    step squared.  Consecutive secant tangents t_{k-1}, t_k of a branch
+    satisfy x_k - x_{k-1} = ds_{k-1} t_k, so the correction
+    (x_k - x_{k-1} - ds_{k-1} t_{k-1}) / ds_{k-1}^2 is (t_k - t_{k-1}) /
+    ds_{k-1}, with ds_{k-1} = (mu_k - mu_{k-1}) / dmu_k; zero at the first
+    step of a branch."""
+
+    def __init__(self):
+        self.t = None
+        self.mu = None
+
+    def step(self, t, mu, dmu):
+        prev_t, prev_mu = self.t, self.mu
+        self.t, self.mu = t, mu
+        if prev_t is None or dmu == 0 or mu == prev_mu or prev_t.shape != t.shape:
+            return torch.zeros_like(t)
+        ds_prev = (mu - prev_mu) / float(dmu)
+        return (t - prev_t) / ds_prev
+
+
 class Recorder:
     """Collects training samples from a plain continuation: pass
     ``recorder.predictor`` as the continuation's predictor (it proposes
     nothing, so the secant predictor runs) and ``recorder.log`` as its log.
-    A sample is (x0, t, mu0, ds, x1, its): the state, tangent and parameter a
-    step started from, the step it was accepted with, the point it converged
-    to and the corrector iterations it took."""
+    A sample is (x0, t, p, mu0, ds, x1, its): the state, tangent, previous
+    correction and parameter a step started from, the step it was accepted
+    with, the point it converged to and the corrector iterations it took."""
 
     def __init__(self):
         self.samples = []
         self._pending = None
         self._ds = None
         self._its = None
+        self._history = _History()
 
     def predictor(self, interface, x0, mu0, dx, dmu, ds):
         if self._pending is not None and self._ds is not None:
-            px, pt, pmu = self._pending
-            self.samples.append({'x0': px, 't': pt, 'mu': pmu, 'ds': self._ds, 'x1': _snapshot(x0),
+            px, pt, pp, pmu = self._pending
+            self.samples.append({'x0': px, 't': pt, 'p': pp, 'mu': pmu, 'ds': self._ds, 'x1': _snapshot(x0),
                                  'its': self._its})
-        self._pending = (_snapshot(x0), _snapshot(dx), float(mu0))
+        t = _snapshot(dx)
+        self._pending = (_snapshot(x0), t, self._history.step(t, float(mu0), dmu), float(mu0))
         self._ds = None
         return None
 
@@ -98,18 +126,20 @@ class Recorder:
 class Surrogate:
     """The network, its Adam state and its scratch buffers (per grid shape)."""
 
-    def __init__(self, dof, channels=32, layers=4, seed=0, device=None):
+    def __init__(self, dof, channels=32, layers=4, seed=0, device=None, history=True):
         if channels not in (16, 32):
             raise ValueError('channels must be 16 or 32')
         if layers < 2:
             raise ValueError('the surrogate needs at least two layers')
-        if 2 * dof + 2 > 32:
-            raise ValueError('at most 15 variables per cell')
+        # inputs: state, tangent, (previous correction,) mu, ds
+        self.history = bool(history)
+        cin = (3 if self.history else 2) * dof + 2
+        if cin > 32:
+            raise ValueError('too many variables per cell for the input layer')
         self.lib = _lib.load()
         self.device = torch.device(device or 'cuda')
         self.dof = dof
         self.layers = layers
-        cin = 2 * dof + 2
         self.kp = [_pad16(cin)] + [channels] * (layers - 1)
         self.np = [channels] * (layers - 1) + [_pad16(dof)]
         real_in = [cin] + [channels] * (layers - 1)
@@ -180,21 +210,29 @@ class Surrogate:
     def _on_device(self, sample):
         """The sample's fields on this surrogate's GPU (samples recorded from
         NumPy continuation vectors are host tensors)."""
-        if all(sample[k].device == self.device for k in ('x0', 't', 'x1')):
+        keys = [k for k in ('x0', 't', 'x1', 'p') if k in sample]
+        if all(sample[k].device == self.device for k in keys):
             return sample
         out = dict(sample)
-        for k in ('x0', 't', 'x1'):
+        for k in keys:
             out[k] = sample[k].to(self.device, dtype=torch.float64).contiguous()
         return out
 
-    def _pack(self, b, x, t, mu, ds):
+    def _pack(self, b, x, t, mu, ds, p=None):
         n = b['ncell'] * self.dof
         check_field(x, n, 'state')
         check_field(t, n, 'tangent')
         sc = self.scales
         sx = (ctypes.c_float * self.dof)(*sc['sx'])
         st = (ctypes.c_float * self.dof)(*sc['st'])
-        _lib.check(self.lib.tf_sg_pack(b['ncell'], self.dof, self.kp[0], _ptr(x), _ptr(t), sx, st,
+        pp, sp = None, None
+        if self.history:
+            if p is None:
+                p = torch.zeros_like(x)
+            check_field(p, n, 'previous correction')
+            pp = p
+            sp = (ctypes.c_float * self.dof)(*sc['sp'])
+        _lib.check(self.lib.tf_sg_pack(b['ncell'], self.dof, self.kp[0], _ptr(x), _ptr(t), _ptr(pp), sx, st, sp,
                                        float(mu * sc['mu']), float(ds * sc['ds']), _ptr(b['x0']), _stream()),
                    'tf_sg_pack')
 
@@ -264,11 +302,12 @@ class Surrogate:
             return [float(v) if v > 1e-300 else 1.0 for v in a]
         xr = rms([s['x0'] for s in samples])
         tr = rms([s['t'] for s in samples])
+        pr = rms([s['p'] if 'p' in s else torch.zeros_like(s['t']) for s in samples])
         dr = rms([(s['x1'] - s['x0'] - s['ds'] * s['t']) / (s['ds'] ** 2) for s in samples])
         mu = max(abs(s['mu']) for s in samples) or 1.0
         ds = max(abs(s['ds']) for s in samples) or 1.0
-        self.scales = {'sx': [1.0 / v for v in xr], 'st': [1.0 / v for v in tr], 'sd': dr,
-                       'mu': 1.0 / mu, 'ds': 1.0 / ds}
+        self.scales = {'sx': [1.0 / v for v in xr], 'st': [1.0 / v for v in tr], 'sp': [1.0 / v for v in pr],
+                       'sd': dr, 'mu': 1.0 / mu, 'ds': 1.0 / ds}
 
     def train(self, samples, dims, steps=300, lr=1e-3, batch=4, seed=0):
         """Adam on the mean-squared scaled target; returns the loss per step
@@ -285,7 +324,7 @@ class Surrogate:
         for it in range(steps):
             for j, i in enumerate(rng.choice(len(samples), size=batch, replace=False)):
                 sample = samples[i]
-                self._pack(b, sample['x0'], sample['t'], sample['mu'], sample['ds'])
+                self._pack(b, sample['x0'], sample['t'], sample['mu'], sample['ds'], sample.get('p'))
                 self._target(b, sample)
                 self._forward(b)
                 self._backward(b, ctypes.c_void_p(losses.data_ptr() + 8 * (it * batch + j)), j > 0)
@@ -301,7 +340,7 @@ class Surrogate:
         b = self._buffers(dims)
         out = torch.zeros(len(samples), dtype=torch.float64, device=self.device)
         for k, sample in enumerate(samples):
-            self._pack(b, sample['x0'], sample['t'], sample['mu'], sample['ds'])
+            self._pack(b, sample['x0'], sample['t'], sample['mu'], sample['ds'], sample.get('p'))
             self._target(b, sample)
             self._forward(b)
             _lib.check(self.lib.tf_sg_loss(b['ncell'], self.dof, self.np[-1], _ptr(b['z'][-1]), _ptr(b['tgt']),
@@ -324,7 +363,7 @@ class Surrogate:
             for smp in g:
                 smp = self._on_device(smp)
                 xs = smp['x0'] + smp['ds'] * smp['t']
-                xl = self.predict(smp['x0'], smp['t'], smp['mu'], smp['ds'], dims)
+                xl = self.predict(smp['x0'], smp['t'], smp['mu'], smp['ds'], dims, smp.get('p'))
                 es = float((smp['x1'] - xs).pow(2).mean().sqrt())
                 el = float((smp['x1'] - xl).pow(2).mean().sqrt())
                 if es > 0:
@@ -351,12 +390,13 @@ class Surrogate:
         return ds * min(max(s / abs(ds), 0.5), 2.0)
 
     # -- inference ------------------------------------------------------------------
-    def predict(self, x, t, mu, ds, dims):
-        """The learned predictor x + ds t + correction (FP64 tensor)."""
+    def predict(self, x, t, mu, ds, dims, p=None):
+        """The learned predictor x + ds t + correction (FP64 tensor); p is the
+        previous step's correction per unit step squared (zero if None)."""
         if self.scales is None:
             raise RuntimeError('the surrogate has not been trained')
         b = self._buffers(dims)
-        self._pack(b, x, t, mu, ds)
+        self._pack(b, x, t, mu, ds, p)
         self._forward(b)
         xp = torch.empty_like(x)
         sc = (ctypes.c_double * self.dof)(*[ds * ds * s for s in self.scales['sd']])
@@ -381,6 +421,7 @@ class LearnedPredictor:
         self.propose_steps = propose_steps
         self.calls = 0
         self.steps_proposed = 0
+        self._history = _History()
 
     # a calibrated network no better than the secant predictor is not used;
     # steps are proposed only by one clearly better
@@ -393,15 +434,18 @@ class LearnedPredictor:
             return None
         sm = net.step_model
         if sm is not None and not sm['eps'] < self.USE_BELOW:
+            if net.history:
+                self._history.step(dx.data.clone(), float(mu0), dmu)
             return None
         self.calls += 1
         dims = (interface.nx, interface.ny, interface.nz)
-        xp = net.predict(x0.data, dx.data, mu0, ds, dims)
+        p = self._history.step(dx.data.clone(), float(mu0), dmu) if net.history else None
+        xp = net.predict(x0.data, dx.data, mu0, ds, dims, p)
         if self.propose_steps and sm is not None and sm['eps'] < self.PROPOSE_BELOW:
             corr = float((xp - x0.data - ds * dx.data).pow(2).mean().sqrt())
             ds_new = net.propose_step(x0.data, dx.data, ds, corr)
             if abs(ds_new / ds - 1.0) > 0.05:
                 self.steps_proposed += 1
-                xp = net.predict(x0.data, dx.data, mu0, ds_new, dims)
+                xp = net.predict(x0.data, dx.data, mu0, ds_new, dims, p)
                 return DeviceVector(xp), mu0 + ds_new * dmu, ds_new
         return DeviceVector(xp), mu0 + ds * dmu
