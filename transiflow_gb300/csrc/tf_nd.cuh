@@ -106,10 +106,10 @@ template <typename T>
 int factor(const tf_nd_plan *p, const double *vals, T *fronts, int32_t *piv, int32_t *info, cudaStream_t s,
            const std::function<int(int)> *after_level);
 
-// Application with the inverted own blocks (tf_nd_inv.cu), one launch pair
-// per height: the forward sweep over heights [0, h_end) or the backward sweep
-// over heights h_end-1 .. 0; y / t of the own rows in `packed` (one value per
-// front index entry).
+// Application with the inverted FP64 own blocks (tf_nd_inv.cu), one launch
+// pair per height: the forward sweep over heights [0, h_end) or the backward
+// sweep over heights h_end-1 .. 0; y / t of the own rows in `packed` (one
+// value per front index entry).
 template <typename T>
 int inv_levels(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int32_t *piv, double *x, double *packed,
                int h_end, bool fwd, cudaStream_t s);

@@ -203,6 +203,133 @@ __global__ void __launch_bounds__(ITHREADS) inv_gemm_kernel(DevPlan P, int node0
     }
 }
 
+// The same GEMMs for FP32 blocks with 128 x 128 output tiles (256 threads,
+// 8 x 8 products per thread from two 16-byte shared-memory loads of each
+// operand per k, k chunks of 16 double-buffered through registers): four
+// times the products per shared-memory load of the 32 x 32 tiles, for the
+// splits whose halves have at least 256 rows.
+constexpr int JT = 128;
+constexpr int JK = 16;
+constexpr int JTHREADS = 256;
+
+template <bool UPPER, int STAGE>
+__global__ void __launch_bounds__(JTHREADS, 2) inv_gemm128_kernel(DevPlan P, int node0, int depth, float *fronts,
+                                                                  float *work, int ld, int64_t front_stride) {
+    const int node = node0 + blockIdx.z;
+    const int n = P.n_own[node], f = P.f[node];
+    int r0, m;
+    if (!split_node(n, depth, blockIdx.y, r0, m)) return;
+    const int m1 = split_at(m), m2 = m - m1;
+    float *F = fronts + P.front_off[node];
+    float *W = work + (int64_t)blockIdx.z * front_stride;
+    const int M = UPPER ? m1 : m2, N = UPPER ? m2 : m1, K = STAGE == 0 ? N : M;
+    const int tiles_n = (N + JT - 1) / JT;
+    const int tm = blockIdx.x / tiles_n, tn = blockIdx.x % tiles_n;
+    const int i0 = tm * JT, j0 = tn * JT;
+    if (i0 >= M) return;
+    int klo = 0, khi = K;
+    if (STAGE == 0) {
+        if (UPPER) khi = min(K, j0 + JT); else klo = j0;
+    } else {
+        if (UPPER) klo = i0; else khi = min(K, i0 + JT);
+    }
+    if (klo >= khi) return;
+    __shared__ __align__(16) float As[2][JK][JT + 4];   // As[k][i]
+    __shared__ __align__(16) float Bs[2][JK][JT + 4];   // Bs[k][j]
+    const int t = threadIdx.x;
+    const int a_k = t % JK, a_i = t / JK;               // A loads: 16 k by 16 rows, 8 passes of 16 rows
+    const int b_j = t % JT, b_k = t / JT;               // B loads: 128 j by 2 k, 8 passes of 2 k
+    const int ty = t / 16, tx = t % 16;                 // products: rows ty*8.., columns tx*8..
+    float ra[8], rb[8];
+    auto gload = [&](int k0) {
+        const int k = k0 + a_k;
+        const bool kok = k >= klo && k < khi;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = i0 + a_i + 16 * q;
+            float a = 0.f;
+            if (kok && i < M) {
+                if (STAGE == 0) {
+                    a = UPPER ? F[(size_t)(r0 + i) * f + r0 + m1 + k] : F[(size_t)(r0 + m1 + i) * f + r0 + k];
+                } else {
+                    const int base = UPPER ? r0 : r0 + m1;
+                    if (UPPER) a = k >= i ? F[(size_t)(base + i) * f + base + k] : 0.f;
+                    else a = k < i ? F[(size_t)(base + i) * f + base + k] : (k == i ? 1.f : 0.f);
+                }
+            }
+            ra[q] = a;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int kb = k0 + b_k + 2 * q, j = j0 + b_j;
+            float b = 0.f;
+            if (kb >= klo && kb < khi && j < N) {
+                if (STAGE == 0) {
+                    const int base = UPPER ? r0 + m1 : r0;
+                    if (UPPER) b = kb <= j ? F[(size_t)(base + kb) * f + base + j] : 0.f;
+                    else b = kb > j ? F[(size_t)(base + kb) * f + base + j] : (kb == j ? 1.f : 0.f);
+                } else {
+                    b = W[(int64_t)(r0 + kb) * ld + j];
+                }
+            }
+            rb[q] = b;
+        }
+    };
+    auto sstore = [&](int buf) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            As[buf][a_k][a_i + 16 * q] = ra[q];
+            Bs[buf][b_k + 2 * q][b_j] = rb[q];
+        }
+    };
+    float acc[8][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+    const int kbeg = klo - (klo % JK);
+    gload(kbeg);
+    sstore(0);
+    __syncthreads();
+    int buf = 0;
+    for (int k0 = kbeg; k0 < khi; k0 += JK) {
+        const bool more = k0 + JK < khi;
+        if (more) gload(k0 + JK);
+#pragma unroll
+        for (int kk = 0; kk < JK; ++kk) {
+            const float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 8]);
+            const float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 8 + 4]);
+            const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 8]);
+            const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 8 + 4]);
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+#pragma unroll
+                for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
+        }
+        if (more) sstore(buf ^ 1);
+        __syncthreads();
+        buf ^= 1;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        const int i = i0 + ty * 8 + u;
+        if (i >= M) continue;
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+            const int j = j0 + tx * 8 + v;
+            if (j >= N) continue;
+            if (STAGE == 0)
+                W[(int64_t)(r0 + i) * ld + j] = acc[u][v];
+            else if (UPPER)
+                F[(size_t)(r0 + i) * f + r0 + m1 + j] = -acc[u][v];
+            else
+                F[(size_t)(r0 + m1 + i) * f + r0 + j] = -acc[u][v];
+        }
+    }
+}
+
 static size_t invert_work_elems(const tf_nd_plan *p) {
     size_t w = 0;
     for (int h = 0; h < p->nlevels; ++h) {
@@ -223,10 +350,28 @@ static void invert_level(const tf_nd_plan *p, const DevPlan &D, int h, T *fronts
     launched();
     const int ld = inv_ld(mo);
     const int64_t stride = (int64_t)mo * ld;
-    for (int depth = inv_depths(mo) - 1; depth >= 0; --depth) {
-        // the largest node at this depth has at most split_at(mo >> depth)-ish rows; bound the
-        // tile grid by the root's halves
-        const int half = split_at(mo);
+    const int depths = inv_depths(mo);
+    // largest segment at each split depth (the first half of a split is the
+    // larger one), which bounds the tile grid of that depth
+    std::vector<int> seg(depths + 1, mo);
+    for (int d = 1; d <= depths; ++d) seg[d] = split_at(seg[d - 1]);
+    for (int depth = depths - 1; depth >= 0; --depth) {
+        const int half = split_at(seg[depth]);
+        if constexpr (sizeof(T) == 4) {
+            if (half >= 2 * JT) {
+                const int tiles = ((half + JT - 1) / JT) * ((half + JT - 1) / JT);
+                dim3 g(tiles, 1 << depth, cnt);
+                inv_gemm128_kernel<false, 0><<<g, JTHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+                launched();
+                inv_gemm128_kernel<false, 1><<<g, JTHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+                launched();
+                inv_gemm128_kernel<true, 0><<<g, JTHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+                launched();
+                inv_gemm128_kernel<true, 1><<<g, JTHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
+                launched();
+                continue;
+            }
+        }
         const int tiles = ((half + IT - 1) / IT) * ((half + IT - 1) / IT);
         dim3 g(tiles, 1 << depth, cnt);
         inv_gemm_kernel<T, false, 0><<<g, ITHREADS, 0, s>>>(D, node0, depth, fronts, work, ld, stride);
@@ -489,71 +634,129 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_kernel(DevPlan P, int node
     }
 }
 
-// The boundary products for FP32 and BF16 factors, FP32 arithmetic.  A warp
-// owns 32 rows and up to ctiles 32-column tiles of one front; for every row
-// its lanes load 32 consecutive columns (one coalesced 128-byte or 64-byte
-// segment), multiply them by the vector entry each lane holds for its
-// column and accumulate per row, so each lane ends with 32 partial sums
-// (one per row); a butterfly of 31 shuffles then leaves lane l with row l's
-// total.  One load instruction per 32 factor entries, against one cp.async
-// per entry in the tile kernel above (whose serial per-lane dot products
-// avoid FP64 shuffles).  The first tile's loads are issued before the wait
-// for the previous launch.
-template <typename S, bool FWD>
-__global__ void __launch_bounds__(BV_THREADS) inv_bnd_rows_kernel(DevPlan P, int node0, int ctiles, const S *fronts,
-                                                                  double *x, double *packed) {
+// ---------------------------------------------------------------------------
+// Application with FP32 or BF16 factors (FP32 products, FP64 sums).  The own
+// triangles and the boundary couplings are the same operation, a block of
+// front rows times a vector over a range of columns, and one kernel does all
+// four per height:
+//   FTRI  y[r]      += s[r] + sum_{c<r}  L11^-1[r][c] s[c],  s[c] = x[g[piv[c]]]
+//   FBND  x[g[r]]   -= sum_c L21[r][c] y[c]                  (r: boundary rows)
+//   BBND  y[r]      -= sum_j U12[r][j] z[g[j]]               (j: boundary columns)
+//   BTRI  z[g[r]]   += sum_{c>=r} U11^-1[r][c] y[c]
+// y and z are vectors of the unknowns' length, addressed by the unknown
+// (y[r] at g[r]), zeroed before the forward sweep; z is the result, copied
+// into x after the backward sweep.  Every contribution is an atomic FP64 add,
+// so a row may be split over any number of CTAs: the top fronts (16385 own
+// rows at 64^3) spread over the whole GPU, and no CTA stages a vector in
+// shared memory.  No launch reads an entry another CTA of the same launch
+// writes.
+//
+// A warp owns AR rows and up to `ctiles` 32-column tiles of one front.  For
+// each row its lanes load 32 consecutive columns (one coalesced segment;
+// rows start at any alignment), multiply by the vector entry each lane holds
+// for its column, and accumulate one partial sum per row; the next tile's
+// loads are issued before the current tile's products, so a warp always has
+// a tile in flight.  A butterfly of shuffles then leaves lane l with row
+// (l mod AR)'s sum.  The factors are read with evict-first loads: they are
+// streamed once per application, while the vectors and indices should stay
+// in L2.
+// ---------------------------------------------------------------------------
+enum { AP_FTRI = 0, AP_FBND = 1, AP_BBND = 2, AP_BTRI = 3 };
+constexpr int AR = 16;                  // rows per warp
+constexpr int AWARPS = 4;
+constexpr int ATHREADS = 32 * AWARPS;
+constexpr int AROWS = AR * AWARPS;      // rows per CTA
+constexpr int ACT = 16;                 // most column tiles per warp
+
+__device__ __forceinline__ float ld_stream(const float *p) { return __ldcs(p); }
+__device__ __forceinline__ float ld_stream(const __nv_bfloat16 *p) { return __bfloat162float(__ldcs(p)); }
+
+template <typename S, int KIND>
+__global__ void __launch_bounds__(ATHREADS, 5) apply_kernel(DevPlan P, int node0, int ctiles, const S *fronts,
+                                                         const int32_t *piv, const double *vin, double *vout) {
+    constexpr bool LOWER = KIND == AP_FTRI, UPPER = KIND == AP_BTRI;
     pdl_trigger();
     const int node = node0 + blockIdx.y;
     const int n = P.n_own[node], f = P.f[node];
-    const int rlo = FWD ? n : 0, rhi = FWD ? f : n;
-    const int clo = FWD ? 0 : n, chi = FWD ? n : f;
-    const int ccols = ctiles * SB;
-    const int rbase = rlo + blockIdx.x * BV_ROWS;
-    const int cbase = clo + blockIdx.z * ccols;
-    if (rbase >= rhi || cbase >= chi) return;
-    const int cend = min(chi, cbase + ccols);
-    const S *F = fronts + P.front_off[node];
-    const int32_t *g = P.idx + P.idx_off[node];
-    double *pk = packed + P.idx_off[node];
+    const int rlo = KIND == AP_FBND ? n : 0, rhi = KIND == AP_FBND ? f : n;
+    const int clo = KIND == AP_BBND ? n : 0, chi = KIND == AP_BBND ? f : n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int r0 = rbase + warp * SB;
-    const int nrows = min(SB, rhi - r0);       // may be <= 0 for the second warp
-    float acc[SB];
-    {
-        // first tile, before the wait (the factors do not change)
-        const int c = cbase + lane;
+    const int r0 = rlo + blockIdx.x * AROWS + warp * AR;
+    const int cbase = clo + blockIdx.z * ctiles * SB;
+    if (r0 >= rhi || cbase >= chi) return;
+    int cstart = cbase, cend = min(chi, cbase + ctiles * SB);
+    // triangles: rows and columns both count from 0, so tiles are 32-aligned
+    // relative to the rows; keep the tiles holding entries of the triangle
+    if (LOWER) cend = min(cend, r0 + AR);                      // c <= r
+    if (UPPER) cstart = max(cstart, r0 & ~(SB - 1));           // c >= r
+    if (cstart >= cend) return;
+    const int nrows = min(AR, rhi - r0);
+    const int nt = (cend - cstart + SB - 1) / SB;
+    const S *F = fronts + P.front_off[node] + (size_t)r0 * f;
+    const int32_t *g = P.idx + P.idx_off[node];
+
+    // entries of this warp's rows in tile c0 (zero outside the rows, the
+    // column range and the triangle; L11's unit diagonal is added in FP64
+    // at the end)
+    auto load = [&](float (&d)[AR], int c0) {
+        const int c = c0 + lane;
         const bool cok = c < cend;
+        const bool diag = (LOWER || UPPER) && c0 + SB > r0 && c0 < r0 + AR;
+        if (!diag) {
 #pragma unroll
-        for (int i = 0; i < SB; ++i) acc[i] = (cok && i < nrows) ? widen(F[(size_t)(r0 + i) * f + c]) : 0.f;
-    }
-    int32_t vi[BV_TILES];
+            for (int i = 0; i < AR; ++i) d[i] = (cok && i < nrows) ? ld_stream(F + (size_t)i * f + c) : 0.f;
+        } else {
 #pragma unroll
-    for (int t = 0; t < BV_TILES; ++t) {
-        const int c = cbase + t * SB + lane;
-        vi[t] = (t < ctiles && c < cend) ? (FWD ? c : g[c]) : -1;
+            for (int i = 0; i < AR; ++i) {
+                const int r = r0 + i;
+                const bool ok = cok && i < nrows && (LOWER ? c < r : c >= r);
+                d[i] = ok ? ld_stream(F + (size_t)i * f + c) : 0.f;
+            }
+        }
+    };
+
+    // the vector entries of the warp's columns: positions before the wait,
+    // values after it, in shared memory (one slot per lane and tile)
+    __shared__ float vbuf[AWARPS][ACT * SB];
+    float *vw = vbuf[warp];
+    float cur[AR];
+    load(cur, cstart);                         // the factors do not change: before the wait
+    int32_t *vpos = reinterpret_cast<int32_t *>(vw);
+    for (int t = 0; t < nt; ++t) {
+        const int c = cstart + t * SB + lane;
+        int32_t q = -1;
+        if (c < cend) q = LOWER ? g[piv[P.piv_off[node] + c]] : g[c];
+        vpos[t * SB + lane] = q;
     }
+    const int32_t gout = lane < nrows ? g[r0 + lane] : 0;
+    // FTRI: s[r] itself, when column r is in this warp's range
+    const bool unit = LOWER && lane < nrows && r0 + lane >= cstart && r0 + lane < cend;
+    const int32_t gdiag = unit ? g[piv[P.piv_off[node] + r0 + lane]] : 0;
     pdl_wait();
-    if (nrows <= 0) return;
-    float v[BV_TILES];
+    for (int t = 0; t < nt; ++t) {
+        const int32_t q = vpos[t * SB + lane];
+        vw[t * SB + lane] = q >= 0 ? (float)vin[q] : 0.f;
+    }
+    float acc[AR];
 #pragma unroll
-    for (int t = 0; t < BV_TILES; ++t) v[t] = vi[t] >= 0 ? (float)(FWD ? pk[vi[t]] : x[vi[t]]) : 0.f;
+    for (int i = 0; i < AR; ++i) acc[i] = 0.f;
 #pragma unroll
-    for (int i = 0; i < SB; ++i) acc[i] *= v[0];
+    for (int t = 0; t < ACT; ++t) {
+        if (t >= nt) break;
+        float nxt[AR];
+        if (t + 1 < nt) load(nxt, cstart + (t + 1) * SB);
+        const float v = vw[t * SB + lane];
 #pragma unroll
-    for (int t = 1; t < BV_TILES; ++t) {
-        if (t >= ctiles || cbase + t * SB >= cend) break;
-        const int c = cbase + t * SB + lane;
-        const bool cok = c < cend;
-        float ld[SB];
+        for (int i = 0; i < AR; ++i) acc[i] = fmaf(cur[i], v, acc[i]);
+        if (t + 1 < nt) {
 #pragma unroll
-        for (int i = 0; i < SB; ++i) ld[i] = (cok && i < nrows) ? widen(F[(size_t)(r0 + i) * f + c]) : 0.f;
-#pragma unroll
-        for (int i = 0; i < SB; ++i) acc[i] = fmaf(ld[i], v[t], acc[i]);
+            for (int i = 0; i < AR; ++i) cur[i] = nxt[i];
+        }
     }
     // transpose-reduce: after the step with offset o a lane keeps o sums, the
-    // half of its rows selected by its lane bit o
+    // half of its rows selected by its lane bit o; then the two half-warps
 #pragma unroll
-    for (int o = SB / 2; o >= 1; o >>= 1) {
+    for (int o = AR / 2; o >= 1; o >>= 1) {
         const bool upper = (lane & o) != 0;
 #pragma unroll
         for (int i = 0; i < o; ++i) {
@@ -562,9 +765,12 @@ __global__ void __launch_bounds__(BV_THREADS) inv_bnd_rows_kernel(DevPlan P, int
             acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
         }
     }
+#pragma unroll
+    for (int o = AR; o < 32; o <<= 1) acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], o);
     if (lane < nrows) {
-        if (FWD) atomicAdd(x + g[r0 + lane], -(double)acc[0]);
-        else atomicAdd(pk + r0 + lane, -(double)acc[0]);
+        double sum = (double)acc[0];
+        if (unit) sum += vin[gdiag];
+        atomicAdd(vout + gout, (KIND == AP_FBND || KIND == AP_BBND) ? -sum : sum);
     }
 }
 
@@ -591,18 +797,15 @@ __global__ void factors_to_bf16_kernel(DevPlan P, int node0, const float *fronts
 
 // The products of one application are launched with programmatic stream
 // serialisation (pdl: every launch but the first of the sequence), so each
-// starts reading its factors while the one before it finishes.
+// starts reading its factors while the one before it finishes.  The three
+// launchers below serve FP64 factors.
 template <typename T, bool FWD>
 static int inv_apply(const DevPlan &D, int node0, int cnt, int mo, const T *fronts, const int32_t *piv, double *x,
                      double *packed, bool pdl, cudaStream_t s) {
     cudaError_t ce = cudaSuccess;
-    // FP32 shuffles are cheap, so single precision always takes a warp per row
-    bool rows = false;
-    if constexpr (sizeof(T) == 8) rows = mo <= VS && cnt >= 256;
-    if (rows) {
-        if constexpr (sizeof(T) == 8)
-            ce = launch_pdl(pdl, inv_apply_rows_kernel<T, FWD>, dim3(1, cnt), dim3(VT), 0, s, D, node0, fronts, piv,
-                            x, packed);
+    if (mo <= VS && cnt >= 256) {
+        ce = launch_pdl(pdl, inv_apply_rows_kernel<T, FWD>, dim3(1, cnt), dim3(VT), 0, s, D, node0, fronts, piv, x,
+                        packed);
     } else {
         const size_t sm = FWD ? (sizeof(double) + sizeof(int32_t)) * (size_t)mo : 0;
         if (sm > 48 * 1024) {
@@ -624,13 +827,31 @@ static int inv_bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, int
     const int wide = rb * cnt * ((cols + BV_TILES * SB - 1) / (BV_TILES * SB));
     const int ctiles = wide >= 4 * nsm ? BV_TILES : 1;
     dim3 grid(rb, cnt, (cols + ctiles * SB - 1) / (ctiles * SB));
-    cudaError_t ce;
-    if constexpr (sizeof(T) <= 4)
-        ce = launch_pdl(pdl, inv_bnd_rows_kernel<T, FWD>, grid, dim3(BV_THREADS), 0, s, D, node0, ctiles, fronts, x,
-                        packed);
-    else
-        ce = launch_pdl(pdl, inv_bnd_kernel<T, FWD>, grid, dim3(BV_THREADS), sizeof(T) * 2 * BV_WARPS * TILE, s, D,
-                        node0, ctiles, fronts, x, packed);
+    const cudaError_t ce = launch_pdl(pdl, inv_bnd_kernel<T, FWD>, grid, dim3(BV_THREADS),
+                                      sizeof(T) * 2 * BV_WARPS * TILE, s, D, node0, ctiles, fronts, x, packed);
+    launched();
+    return ce == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+// One product of the FP32 / BF16 application over every front of a height
+// (at most `rows` rows and `cols` columns per front).  A warp takes up to ACT
+// column tiles; fewer when the height would otherwise give the GPU fewer than
+// about four waves of warps.
+template <typename S, int KIND>
+static int apply_launch(const DevPlan &D, int node0, int cnt, int rows, int cols, int nsm, const S *fronts,
+                        const int32_t *piv, const double *vin, double *vout, bool pdl, cudaStream_t s) {
+    if (rows <= 0 || cols <= 0) return TF_OK;
+    constexpr bool TRI = KIND == AP_FTRI || KIND == AP_BTRI;
+    const int64_t target = 64 * (int64_t)nsm;
+    int ct = ACT;
+    for (; ct > 1; ct /= 2) {
+        int64_t warps = (int64_t)((rows + AR - 1) / AR) * cnt * ((cols + ct * SB - 1) / (ct * SB));
+        if (TRI) warps /= 2;
+        if (warps >= target) break;
+    }
+    const dim3 grid((rows + AROWS - 1) / AROWS, cnt, (cols + ct * SB - 1) / (ct * SB));
+    const cudaError_t ce = launch_pdl(pdl, apply_kernel<S, KIND>, grid, dim3(ATHREADS), 0, s, D, node0, ct, fronts,
+                                      piv, vin, vout);
     launched();
     return ce == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
@@ -661,15 +882,47 @@ int inv_levels(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int
     return cuda_status();
 }
 
+// FP64 factors: the products above, with y / t in `packed`.
+// FP32 and BF16 factors: apply_kernel, with y and z in the first 2n doubles
+// of the scratch.
 template <typename T>
 static int solve_inv(const tf_nd_plan *p, const DevPlan &D, const T *fronts, const int32_t *piv, double *x,
-                     double *packed, cudaStream_t s) {
-    int e = inv_levels<T>(p, D, fronts, piv, x, packed, p->nlevels, true, s);
-    return e ? e : inv_levels<T>(p, D, fronts, piv, x, packed, p->nlevels, false, s);
+                     double *scratch, cudaStream_t s) {
+    if constexpr (sizeof(T) == 8) {
+        int e = inv_levels<T>(p, D, fronts, piv, x, scratch, p->nlevels, true, s);
+        return e ? e : inv_levels<T>(p, D, fronts, piv, x, scratch, p->nlevels, false, s);
+    } else {
+        int dev = 0, nsm = 0, e = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return TF_ERR_CUDA;
+        const size_t n = (size_t)p->n;
+        double *y = scratch, *z = scratch + n;
+        if (cudaMemsetAsync(scratch, 0, 2 * n * sizeof(double), s) != cudaSuccess) return TF_ERR_CUDA;
+        bool first = true;   // the first launch waits for the memset
+        for (int h = 0; h < p->nlevels; ++h) {
+            const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
+            const int mo = p->max_own[h], mf = p->max_f[h];
+            if (cnt <= 0 || mo <= 0) continue;
+            const int nb = cnt == 1 ? mf - mo : mf;     // boundary rows of a front, at most
+            if ((e = apply_launch<T, AP_FTRI>(D, node0, cnt, mo, mo, nsm, fronts, piv, x, y, !first, s))) return e;
+            first = false;
+            if ((e = apply_launch<T, AP_FBND>(D, node0, cnt, nb, mo, nsm, fronts, piv, y, x, true, s))) return e;
+        }
+        for (int h = p->nlevels - 1; h >= 0; --h) {
+            const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
+            const int mo = p->max_own[h], mf = p->max_f[h];
+            if (cnt <= 0 || mo <= 0) continue;
+            const int nb = cnt == 1 ? mf - mo : mf;
+            if ((e = apply_launch<T, AP_BBND>(D, node0, cnt, mo, nb, nsm, fronts, piv, z, y, true, s))) return e;
+            if ((e = apply_launch<T, AP_BTRI>(D, node0, cnt, mo, mo, nsm, fronts, piv, y, z, true, s))) return e;
+        }
+        if (cudaMemcpyAsync(x, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            return TF_ERR_CUDA;
+        return cuda_status();
+    }
 }
 
-template int inv_levels<float>(const tf_nd_plan *, const DevPlan &, const float *, const int32_t *, double *, double *,
-                               int, bool, cudaStream_t);
 template int inv_levels<double>(const tf_nd_plan *, const DevPlan &, const double *, const int32_t *, double *,
                                 double *, int, bool, cudaStream_t);
 
@@ -704,7 +957,8 @@ extern "C" size_t tf_nd_solve_inv_workspace_bytes(const tf_nd_plan *plan) {
         cudaGetLastError();
         return 0;
     }
-    return (size_t)len * sizeof(double);
+    // FP64 factors: one double per front index entry; FP32 / BF16: 2n
+    return (size_t)std::max<int64_t>(len, 2 * (int64_t)plan->n) * sizeof(double);
 }
 
 extern "C" int tf_nd_factor_inv_f64(const tf_nd_plan *plan, const double *d_vals, double *d_fronts, int32_t *d_piv,
