@@ -212,6 +212,8 @@ def _free():
 
 def _branch(itf, x0, args, predictor=None, log=None):
     from transiflow_gb300 import Continuation
+    if predictor is not None:
+        predictor.reset()       # a new branch: no history
     cont = Continuation(itf, newton_tolerance=1e-8, quiet=True, predictor=predictor, log=log)
     itf.set_parameter('Reynolds Number', 0.0)
     x = cont.newton(x0)
@@ -232,7 +234,7 @@ def train_predictor(args):
     learned predictor trained on all of their points."""
     import torch
     from transiflow_gb300 import Continuation, Interface
-    from transiflow_gb300.surrogate import Recorder, Surrogate
+    from transiflow_gb300.surrogate import Recorder, Surrogate, regular_steps
     t0 = time.perf_counter()
     groups = []
     stalls = []
@@ -262,26 +264,17 @@ def train_predictor(args):
                     raise
                 stalls.append((n, seed, float(itf.get_parameter('Reynolds Number'))))
             # regular steps only: near a singular point the accepted steps
-            # shrink to ~0.01 and (x1 - secant) / ds^2 explodes
-            # and not the first step from Re = 0, whose correction is not of
-            # order ds^2 (the reference's Re = 0 -> 1 viscosity substitution)
-            kept = [smp for smp in rec.samples if smp['ds'] >= 0.25 * args.train_ds and (smp['its'] or 0) >= 1
-                    and smp['mu'] > 0.0]
+            # shrink to ~0.01; the first steps from Re = 0 (the reference's
+            # Re = 0 -> 1 viscosity substitution) and other steps the
+            # three-point history does not describe are dropped by
+            # regular_steps
+            kept = regular_steps([smp for smp in rec.samples
+                                  if smp['ds'] >= 0.25 * args.train_ds and (smp['its'] or 0) >= 1])
             dropped += len(rec.samples) - len(kept)
             groups.append(((n, n, n), kept))
             del itf, cont, x0
             _free()
     branches_s = time.perf_counter() - t0
-    # robust to the remaining outliers: drop samples whose scaled correction
-    # (x1 - secant) / ds^2 is more than ten times the median's
-    size = {id(smp): float((smp['x1'] - smp['x0'] - smp['ds'] * smp['t']).pow(2).mean().sqrt()) / smp['ds'] ** 2
-            for _, g in groups for smp in g}
-    med = float(np.median(list(size.values()))) if size else 0.0
-    outliers = 0
-    for k, (dims, g) in enumerate(groups):
-        keep = [smp for smp in g if size[id(smp)] <= 10.0 * med]
-        outliers += len(g) - len(keep)
-        groups[k] = (dims, keep)
     net = Surrogate(4)
     net.fit_scales([smp for _, g in groups for smp in g])
     t1 = time.perf_counter()
@@ -297,7 +290,6 @@ def train_predictor(args):
     info = {'branches': len(groups), 'points': sum(len(g) for _, g in groups), 'branches_s': branches_s,
             'step_model': step_model,
             'ended_at_singular_point': stalls, 'irregular_points_dropped': dropped,
-            'outliers_dropped': outliers,
             'train_s': time.perf_counter() - t1, 'adam_steps': args.train_rounds * args.train_steps * len(groups),
             'final_loss': losses[-1] if losses else None, 'parameters': net.parameters()}
     return net, info
@@ -384,7 +376,8 @@ def learned_arm(args, net, rank, local):
            'branch': {'points': cont.stats['points'], 'rhs': cont.stats['rhs'], 'jacobian': cont.stats['jacobian'],
                       'solve': cont.stats['solve'], 'learned_accepted': cont.stats['learned_accepted'],
                       'learned_rejected': cont.stats['learned_rejected'], 'per_step_solver': per,
-                      'steps_proposed': pred.steps_proposed,
+                      'steps_proposed': pred.steps_proposed, 'learned_used': pred.used,
+                      'learned_over_secant_error': [round(r, 4) for r in pred.ratios],
                       'mus': [r['mu'] for r in logs[-1]], 'step_s': t_dev}}
     out['end_state'] = _polish(itf, x, mu)
     return out, itf

@@ -109,8 +109,12 @@ def test_recorder_collects_consecutive_steps():
     for k, sm in enumerate(smp):
         assert sm['ds'] == steps[k]['ds']
     # the previous-correction input: zero at the first step, then the
-    # previous sample's (x1 - x0 - ds t) / ds^2
-    assert torch.count_nonzero(smp[0]['p']) == 0
+    # previous sample's (x1 - x0 - ds t) / ds^2; its weight phi in the
+    # quadratic extrapolation for the step taken (the first tangent is exact)
+    assert torch.count_nonzero(smp[0]['p']) == 0 and smp[0]['phi'] == 0.0
+    for k in range(1, len(smp)):
+        h, h0, ds = smp[k - 1]['ds'], smp[k - 2]['ds'] if k >= 2 else 0.0, smp[k]['ds']
+        assert smp[k]['phi'] == pytest.approx(h * (ds + h) / (ds * (h0 + h)), rel=1e-12)
     for a, b in zip(smp, smp[1:]):
         want = (a['x1'] - a['x0'] - a['ds'] * a['t']) / a['ds'] ** 2
         assert torch.allclose(b['p'], want, rtol=1e-9, atol=1e-12)
@@ -119,6 +123,32 @@ def test_recorder_collects_consecutive_steps():
         assert np.all(np.isfinite(x1))
         r = np.roots([1, 0, 1, -sm['mu']]).real.max()
         assert np.allclose(sm['x0'].numpy(), [r, 0.5 * sm['mu']], rtol=1e-9, atol=1e-9)
+
+
+def test_quadratic_extrapolation_is_exact_on_a_parabola():
+    """The history's p and phi reproduce a quadratic branch exactly: for
+    x(s) = a + b s + c s^2 sampled at unequal steps, with the exact tangent
+    at the first point and secant tangents after it, x_k + ds t_k + ds^2 phi
+    p lands on x(s_k + ds) for every next step ds."""
+    from transiflow_gb300.surrogate import _History
+    g = torch.Generator().manual_seed(3)
+    a, b, c = (torch.randn(5, dtype=torch.float64, generator=g) for _ in range(3))
+
+    def x(s):
+        return a + b * s + c * s * s
+    s_pts = [0.0, 0.7, 1.9, 2.4, 3.9, 4.2]
+    hist = _History()
+    t = b.clone()                    # exact tangent at s = 0 (dmu = 1: mu is s)
+    for k, sk in enumerate(s_pts):
+        if k > 0:
+            t = (x(sk) - x(s_pts[k - 1])) / (sk - s_pts[k - 1])
+        p = hist.step(t, sk, 1.0)
+        if k == 0:
+            assert torch.count_nonzero(p) == 0 and hist.phi(1.0) == 0.0
+            continue
+        for ds in (0.3, 1.0, 2.5):
+            pred = x(sk) + ds * t + ds * ds * hist.phi(ds) * p
+            assert torch.allclose(pred, x(sk + ds), rtol=0, atol=1e-12), (k, ds)
 
 
 # -- GPU: the kernels against the oracle ---------------------------------------
@@ -266,8 +296,9 @@ def _branch_samples():
 def trained():
     if not torch.cuda.is_available():
         pytest.skip('needs a GPU')
-    from transiflow_gb300.surrogate import Surrogate
+    from transiflow_gb300.surrogate import Surrogate, regular_steps
     itf, x0, x_plain, stats, samples = _branch_samples()
+    samples = regular_steps(samples)
     s = Surrogate(itf.dof, seed=0)
     s.fit_scales(samples)
     before = s.evaluate(samples, (16, 16, 1))
@@ -279,11 +310,11 @@ def trained():
 
 @pytest.mark.gpu
 def test_training_reduces_the_predictor_error(trained):
-    """Trained on the branch points of a plain continuation (2D lid-driven
-    cavity 16x16, Re 0 -> 2000, ds = 100), the network's predictor is
-    closer to the corrected points than the secant predictor it starts
-    from.  The scaled error of the untrained network is the secant
-    predictor's (about 1 by construction)."""
+    """Trained on the regular branch points of a plain continuation (2D
+    lid-driven cavity 16x16, Re 0 -> 2000, ds = 100), the network's
+    predictor is closer to the corrected points than the quadratic
+    extrapolation it starts from (the untrained network's scaled error is
+    the quadratic's residual relative to its correction)."""
     before, after = trained['before'], trained['after']
     print('samples %d, secant error %.4f, learned error %.4f, final training loss %.4f'
           % (len(trained['samples']), before.mean(), after.mean(), trained['losses'][-10:].mean()))
@@ -368,8 +399,9 @@ def test_samples_from_two_grid_sizes_train_one_network():
         a = np.concatenate([s[key].cpu().numpy().reshape(-1, 3) for s in samples])
         return np.sqrt((a ** 2).mean(axis=0))
     xr, tr = rms('x0'), rms('t')
-    d = np.concatenate([((s['x1'] - s['x0'] - s['ds'] * s['t']) / s['ds'] ** 2).cpu().numpy().reshape(-1, 3)
-                        for s in samples])
+    # residual mode: the target is what the quadratic extrapolation misses
+    d = np.concatenate([((s['x1'] - s['x0'] - s['ds'] * s['t']) / s['ds'] ** 2 - s['phi'] * s['p'])
+                        .cpu().numpy().reshape(-1, 3) for s in samples])
     dr = np.sqrt((d ** 2).mean(axis=0))
     assert np.allclose(net.scales['sx'], 1.0 / xr, rtol=1e-6)
     assert np.allclose(net.scales['st'], 1.0 / tr, rtol=1e-6)
@@ -413,15 +445,18 @@ def test_predictor_can_propose_the_step_size(quality):
 
 @pytest.mark.gpu
 def test_learned_predictor_on_an_unseen_grid():
-    """Trained on plain branches of 2D lid-driven cavities 12^2 and 16^2 (Re
-    0 -> 2000), the predictor is used on a 24^2 cavity it has not seen: the
-    branch ends at the plain branch's solution, every point has ||F|| <=
-    1e-8, the calibrated error is below the secant predictor's, and the
-    corrector work of both runs is printed (the gain out of sample)."""
+    """Trained on the regular steps of plain branches of 2D lid-driven
+    cavities 12^2 and 16^2 (Re 0 -> 2000, ds = 100), the predictor is used on
+    a 24^2 cavity it has not seen, with steps growing past the trained ones:
+    the branch ends at the plain branch's solution, every point has ||F||
+    <= 1e-8, the calibrated error is below the secant predictor's, and on
+    the unseen grid the learned prediction of a step is typically (median
+    over the branch) well below the secant's error.  The corrector work of
+    both runs is printed."""
     import contextlib
     import io
     from transiflow_gb300 import Continuation, Interface
-    from transiflow_gb300.surrogate import LearnedPredictor, Recorder, Surrogate
+    from transiflow_gb300.surrogate import LearnedPredictor, Recorder, Surrogate, regular_steps
     groups = []
     for n in (12, 16):
         itf = Interface({'CUDA': {'Tolerance': 1e-10}}, n, n)
@@ -429,7 +464,7 @@ def test_learned_predictor_on_an_unseen_grid():
         cont = Continuation(itf, newton_tolerance=1e-8, predictor=rec.predictor, log=rec.log)
         with contextlib.redirect_stdout(io.StringIO()):
             cont.continuation(cont.newton(itf.vector()), 'Reynolds Number', 0.0, 2000.0, 100.0, ds_max=100.0)
-        groups.append(((n, n, 1), [s for s in rec.samples if s['mu'] > 0 and (s['its'] or 0) >= 1]))
+        groups.append(((n, n, 1), regular_steps(rec.samples)))
     net = Surrogate(3)
     net.fit_scales([s for _, g in groups for s in g])
     for r in range(4):
@@ -447,11 +482,14 @@ def test_learned_predictor_on_an_unseen_grid():
         assert abs(mu - 2000.0) < 1e-3 and max(f for f in fn if f is not None) <= 1e-8
         itf.set_parameter('Reynolds Number', mu)
         xe = Continuation(itf, quiet=True).newton(x, 1e-12).numpy()
-        runs[name] = (dict(cont.stats), xe, getattr(pred, 'steps_proposed', 0))
+        runs[name] = (dict(cont.stats), xe, pred)
     print('step model', model)
-    for name, (st, _, sp) in runs.items():
+    for name, (st, _, pred) in runs.items():
         print(name, {k: st[k] for k in ('points', 'jacobian', 'solve', 'learned_accepted', 'learned_rejected')},
-              'steps proposed', sp)
+              'steps proposed', getattr(pred, 'steps_proposed', 0))
+    ratios = runs['learned'][2].ratios
+    print('learned / secant error on the unseen grid, per step:', [round(r, 3) for r in ratios])
     assert model['eps'] < 1.0
+    assert len(ratios) >= 5 and float(np.median(ratios)) < 0.7
     assert np.linalg.norm(runs['learned'][1] - runs['plain'][1]) <= 1e-8 * np.linalg.norm(runs['plain'][1])
     assert runs['learned'][0]['learned_accepted'] > 0

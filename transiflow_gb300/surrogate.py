@@ -1,16 +1,23 @@
 """Learned continuation predictor: a convolutional surrogate trained on the
 branch points that plain continuation computes.
 
-The network reads the current state ``x``, the secant tangent ``t``, the
-previous step's correction of the secant predictor per unit step squared
-``p`` (the change of the secant tangent over the last step -- a quadratic
-extrapolation the network refines, since a 3x3x3 stencil network alone sees
-only nine cells of what is a global curvature), the parameter ``mu`` and the
-step ``ds`` on the cell grid and proposes the correction to the secant
-predictor ``x + ds*t``, and through it the next step size.  The Newton corrector of the
+The predictor is a three-point quadratic extrapolation of the branch plus a
+learned residual.  With the secant tangents t_{k-1}, t_k of the last two
+steps (lengths h0, h) the quadratic through the last three points corrects
+the secant predictor ``x + ds*t`` by ``ds**2 * phi * p`` with
+``p = (t_k - t_{k-1}) / h`` (the previous step's correction per unit step
+squared) and ``phi = h (ds + h) / (ds (h0 + h))`` (1 for equal steps; after
+the first, exact tangent h0 = 0).  The network reads the current state
+``x``, the secant tangent ``t``, ``p``, the parameter ``mu`` and the step
+``ds`` on the cell grid and proposes what the quadratic still misses; a
+3x3x3 stencil network alone sees only a few cells of what is a global
+curvature, the extrapolation carries it.  Through the predicted correction
+it also proposes the next step size.  The Newton corrector of the
 continuation judges every point; the secant predictor is the fallback
 whenever the corrector started from the learned predictor does not converge
-within ``Continuation(learned_newton_iterations=4)`` iterations.
+within ``Continuation(learned_newton_iterations=4)`` iterations, and
+``LearnedPredictor`` uses the network only while its prediction of the last
+step beat the secant's.
 
 Architecture: ``layers`` 3x3x3 convolutions over the cell grid (a 2D grid is
 a grid one cell thick), ``channels`` channels between them, ReLU after every
@@ -20,9 +27,10 @@ variable, mu and ds as constant fields; ``2*dof + 2`` without p), outputs
 backward and Adam run in libtfcuda kernels (``tf_sg_*``): BF16 operands with
 FP32 accumulation on the tensor cores, FP32 master weights.  Inputs and
 targets are scaled per variable with statistics of the training samples; the
-target is the corrector's displacement from the secant predictor divided by
-``ds**2`` (the order of the secant predictor's error), so the zero-initialised
-last layer starts the network at exactly the secant predictor.
+target is the corrector's displacement from the quadratic predictor divided
+by ``ds**2`` (the order of the secant predictor's error), so the
+zero-initialised last layer starts the network at exactly the quadratic
+predictor (the secant one without ``p``).
 
 The reference has no counterpart: its continuation predicts with the secant
 only (transiflow/Continuation.py:258-260).
@@ -37,7 +45,7 @@ import torch
 from . import _lib
 from .vector import DeviceVector, _stream
 
-__all__ = ['Surrogate', 'Recorder', 'LearnedPredictor']
+__all__ = ['Surrogate', 'Recorder', 'LearnedPredictor', 'regular_steps']
 
 
 def _pad16(c):
@@ -72,34 +80,52 @@ def check_field(t, n, name='field'):
         raise ValueError('%s has %d values, the grid needs %d' % (name, t.numel(), n))
 
 
+def _phi(h, h0, ds):
+    """Weight of p in the quadratic extrapolation through the last three
+    points for the next step ds (h: the last step, h0: the one before, 0
+    when the earlier tangent was the exact one at the first point)."""
+    if h is None or h0 is None or ds == 0 or abs(h0 + h) <= 1e-12 * abs(h):
+        return 0.0
+    return h * (ds + h) / (ds * (h0 + h))
+
+
 class _History:
     """The previous step's correction of the secant predictor, per unit
     step squared.  Consecutive secant tangents t_{k-1}, t_k of a branch
     satisfy x_k - x_{k-1} = ds_{k-1} t_k, so the correction
     (x_k - x_{k-1} - ds_{k-1} t_{k-1}) / ds_{k-1}^2 is (t_k - t_{k-1}) /
     ds_{k-1}, with ds_{k-1} = (mu_k - mu_{k-1}) / dmu_k; zero at the first
-    step of a branch."""
+    step of a branch.  Also keeps the last two step lengths for phi."""
 
     def __init__(self):
         self.t = None
         self.mu = None
+        self.h = None
+        self.h0 = None
 
     def step(self, t, mu, dmu):
         prev_t, prev_mu = self.t, self.mu
         self.t, self.mu = t, mu
         if prev_t is None or dmu == 0 or mu == prev_mu or prev_t.shape != t.shape:
+            self.h = self.h0 = None
             return torch.zeros_like(t)
         ds_prev = (mu - prev_mu) / float(dmu)
+        # the first tangent of a branch is exact: a double node, h0 = 0
+        self.h0, self.h = (self.h if self.h is not None else 0.0), ds_prev
         return (t - prev_t) / ds_prev
+
+    def phi(self, ds):
+        return _phi(self.h, self.h0, ds)
 
 
 class Recorder:
     """Collects training samples from a plain continuation: pass
     ``recorder.predictor`` as the continuation's predictor (it proposes
     nothing, so the secant predictor runs) and ``recorder.log`` as its log.
-    A sample is (x0, t, p, mu0, ds, x1, its): the state, tangent, previous
-    correction and parameter a step started from, the step it was accepted
-    with, the point it converged to and the corrector iterations it took."""
+    A sample is (x0, t, p, phi, mu0, ds, x1, its): the state, tangent,
+    previous correction and parameter a step started from, the weight of p
+    in the quadratic extrapolation for the step it was accepted with, that
+    step, the point it converged to and the corrector iterations it took."""
 
     def __init__(self):
         self.samples = []
@@ -110,11 +136,12 @@ class Recorder:
 
     def predictor(self, interface, x0, mu0, dx, dmu, ds):
         if self._pending is not None and self._ds is not None:
-            px, pt, pp, pmu = self._pending
-            self.samples.append({'x0': px, 't': pt, 'p': pp, 'mu': pmu, 'ds': self._ds, 'x1': _snapshot(x0),
-                                 'its': self._its})
+            px, pt, pp, pmu, h, h0 = self._pending
+            self.samples.append({'x0': px, 't': pt, 'p': pp, 'phi': _phi(h, h0, self._ds), 'mu': pmu,
+                                 'ds': self._ds, 'x1': _snapshot(x0), 'its': self._its})
         t = _snapshot(dx)
-        self._pending = (_snapshot(x0), t, self._history.step(t, float(mu0), dmu), float(mu0))
+        pp = self._history.step(t, float(mu0), dmu)
+        self._pending = (_snapshot(x0), t, pp, float(mu0), self._history.h, self._history.h0)
         self._ds = None
         return None
 
@@ -123,16 +150,38 @@ class Recorder:
         self._its = record.get('newton_iterations')
 
 
+def regular_steps(samples):
+    """The samples a three-point history describes: a nonzero quadratic
+    correction phi p that brings the predictor closer to the converged point
+    than the secant predictor.  This drops the first steps of a branch and
+    steps across irregular stretches (from a Stokes state, at a fold), whose
+    corrections are unrelated to the history; the predictor's online guard
+    keeps the secant there."""
+    out = []
+    for smp in samples:
+        p, phi = smp.get('p'), smp.get('phi', 0.0)
+        if p is None or not phi:
+            continue
+        xs = smp['x0'] + smp['ds'] * smp['t']
+        es = float((smp['x1'] - xs).pow(2).mean().sqrt())
+        eq = float((smp['x1'] - xs - (smp['ds'] ** 2 * phi) * p).pow(2).mean().sqrt())
+        if 0 < eq < es:
+            out.append(smp)
+    return out
+
+
 class Surrogate:
     """The network, its Adam state and its scratch buffers (per grid shape)."""
 
-    def __init__(self, dof, channels=32, layers=4, seed=0, device=None, history=True):
+    def __init__(self, dof, channels=32, layers=4, seed=0, device=None, history=True, residual=True):
         if channels not in (16, 32):
             raise ValueError('channels must be 16 or 32')
         if layers < 2:
             raise ValueError('the surrogate needs at least two layers')
         # inputs: state, tangent, (previous correction,) mu, ds
         self.history = bool(history)
+        # learn the residual of the quadratic extrapolation (needs p)
+        self.residual = bool(residual) and self.history
         cin = (3 if self.history else 2) * dof + 2
         if cin > 32:
             raise ValueError('too many variables per cell for the input layer')
@@ -198,6 +247,7 @@ class Surrogate:
              'dzh': [torch.empty(ncell * n, dtype=torch.bfloat16, **dev) for n in self.np],
              'da': [torch.empty(ncell * n, dtype=torch.float32, **dev) for n in self.np[:L - 1]],
              'tgt': torch.empty(ncell * self.dof, dtype=torch.float32, **dev),
+             'xb': torch.empty(ncell * self.dof, dtype=torch.float64, **dev),
              'loss': torch.zeros(1, dtype=torch.float64, **dev)}
         lw = self.lib.tf_sg_loss_workspace_bytes(ncell, self.np[-1])
         ww = max(self.lib.tf_sg_wgrad_workspace_bytes(ncell, kp, np_) for kp, np_ in zip(self.kp, self.np))
@@ -218,7 +268,30 @@ class Surrogate:
             out[k] = sample[k].to(self.device, dtype=torch.float64).contiguous()
         return out
 
-    def _pack(self, b, x, t, mu, ds, p=None):
+    def _based(self, b, x, ds, p, phi):
+        """x + ds^2 phi p (into the scratch) when the network learns the
+        residual of the quadratic extrapolation, else x."""
+        if not self.residual or p is None or not phi:
+            return x
+        n = b['ncell'] * self.dof
+        check_field(p, n, 'previous correction')
+        _lib.check(self.lib.tf_vec_axpby(n, 1.0, _ptr(x), float(ds * ds * phi), _ptr(p), _ptr(b['xb']), _stream()),
+                   'tf_vec_axpby')
+        return b['xb']
+
+    def _pscale(self, p, phi):
+        """Per-variable RMS of the quadratic correction phi p (the scale of
+        the residual the network learns), or None when it is zero."""
+        if not self.residual or p is None or not phi:
+            return None
+        r = (p.view(-1, self.dof).pow(2).mean(dim=0).sqrt() * abs(phi)).cpu().tolist()
+        return r if max(r) > 0 else None
+
+    def _pack(self, b, x, t, mu, ds, p=None, phi=0.0, ps='auto'):
+        """Packs the network input; returns the per-variable residual scales
+        of this sample (residual mode; None when the quadratic correction is
+        zero, and then the network's output is not used).  ``ps`` may pass
+        scales computed before (training reuses them every step)."""
         n = b['ncell'] * self.dof
         check_field(x, n, 'state')
         check_field(t, n, 'tangent')
@@ -226,23 +299,41 @@ class Surrogate:
         sx = (ctypes.c_float * self.dof)(*sc['sx'])
         st = (ctypes.c_float * self.dof)(*sc['st'])
         pp, sp = None, None
+        if not (self.history and self.residual):
+            ps = None
         if self.history:
             if p is None:
                 p = torch.zeros_like(x)
             check_field(p, n, 'previous correction')
             pp = p
-            sp = (ctypes.c_float * self.dof)(*sc['sp'])
+            if self.residual:
+                # p at unit RMS per variable: the network sees the shape of
+                # the curvature, whatever its size
+                ps = self._pscale(p, phi) if isinstance(ps, str) else ps
+                sp = (ctypes.c_float * self.dof)(*[abs(phi) / r if ps and r > 0 else 0.0
+                                                   for r in (ps or [0.0] * self.dof)])
+            else:
+                sp = (ctypes.c_float * self.dof)(*sc['sp'])
         _lib.check(self.lib.tf_sg_pack(b['ncell'], self.dof, self.kp[0], _ptr(x), _ptr(t), _ptr(pp), sx, st, sp,
                                        float(mu * sc['mu']), float(ds * sc['ds']), _ptr(b['x0']), _stream()),
                    'tf_sg_pack')
+        return ps
 
-    def _target(self, b, sample):
+    def _out_scales(self, ds, ps):
+        """Per-variable factors from the network's output to the state: ds^2
+        times the residual scale (residual mode) or the global target scale."""
+        if self.residual:
+            return [ds * ds * r for r in (ps or [0.0] * self.dof)]
+        return [ds * ds * v for v in self.scales['sd']]
+
+    def _target(self, b, sample, ps=None):
         n = b['ncell'] * self.dof
         for k in ('x0', 't', 'x1'):
             check_field(sample[k], n, 'sample ' + k)
         ds = sample['ds']
-        inv = (ctypes.c_double * self.dof)(*[1.0 / (ds * ds * s) for s in self.scales['sd']])
-        _lib.check(self.lib.tf_sg_target(b['ncell'], self.dof, _ptr(sample['x0']), _ptr(sample['t']),
+        x0 = self._based(b, sample['x0'], ds, sample.get('p'), sample.get('phi', 0.0))
+        inv = (ctypes.c_double * self.dof)(*[1.0 / v if v > 0 else 0.0 for v in self._out_scales(ds, ps)])
+        _lib.check(self.lib.tf_sg_target(b['ncell'], self.dof, _ptr(x0), _ptr(sample['t']),
                                          _ptr(sample['x1']), float(ds), inv, _ptr(b['tgt']), _stream()),
                    'tf_sg_target')
 
@@ -303,7 +394,11 @@ class Surrogate:
         xr = rms([s['x0'] for s in samples])
         tr = rms([s['t'] for s in samples])
         pr = rms([s['p'] if 'p' in s else torch.zeros_like(s['t']) for s in samples])
-        dr = rms([(s['x1'] - s['x0'] - s['ds'] * s['t']) / (s['ds'] ** 2) for s in samples])
+        def base(s):
+            if self.residual and 'p' in s and s.get('phi'):
+                return s['phi'] * s['p']
+            return 0.0
+        dr = rms([(s['x1'] - s['x0'] - s['ds'] * s['t']) / (s['ds'] ** 2) - base(s) for s in samples])
         mu = max(abs(s['mu']) for s in samples) or 1.0
         ds = max(abs(s['ds']) for s in samples) or 1.0
         self.scales = {'sx': [1.0 / v for v in xr], 'st': [1.0 / v for v in tr], 'sp': [1.0 / v for v in pr],
@@ -321,27 +416,33 @@ class Surrogate:
         rng = np.random.default_rng(seed)
         batch = min(batch, len(samples))
         losses = torch.zeros(steps * batch, dtype=torch.float64, device=self.device)
+        scales = [self._pscale(smp.get('p'), smp.get('phi', 0.0)) for smp in samples]
         for it in range(steps):
             for j, i in enumerate(rng.choice(len(samples), size=batch, replace=False)):
                 sample = samples[i]
-                self._pack(b, sample['x0'], sample['t'], sample['mu'], sample['ds'], sample.get('p'))
-                self._target(b, sample)
+                ps = self._pack(b, sample['x0'], sample['t'], sample['mu'], sample['ds'], sample.get('p'),
+                                sample.get('phi', 0.0), scales[i])
+                self._target(b, sample, ps)
                 self._forward(b)
                 self._backward(b, ctypes.c_void_p(losses.data_ptr() + 8 * (it * batch + j)), j > 0)
             self._adam(lr, batch)
         return losses.view(steps, batch).mean(dim=1).cpu().numpy()
 
     def evaluate(self, samples, dims):
-        """Scaled mean-squared error of the predictor per sample (1.0 is the
-        secant predictor's error level)."""
+        """Scaled mean-squared error of the network per sample: of the
+        residual of the quadratic extrapolation relative to the quadratic
+        correction (residual mode), else of the secant predictor's
+        correction relative to its training RMS (1.0: the secant
+        predictor's error level)."""
         if self.scales is None:
             raise RuntimeError('fit_scales() or train() sets the scales first')
         samples = [self._on_device(smp) for smp in samples]
         b = self._buffers(dims)
         out = torch.zeros(len(samples), dtype=torch.float64, device=self.device)
         for k, sample in enumerate(samples):
-            self._pack(b, sample['x0'], sample['t'], sample['mu'], sample['ds'], sample.get('p'))
-            self._target(b, sample)
+            ps = self._pack(b, sample['x0'], sample['t'], sample['mu'], sample['ds'], sample.get('p'),
+                            sample.get('phi', 0.0))
+            self._target(b, sample, ps)
             self._forward(b)
             _lib.check(self.lib.tf_sg_loss(b['ncell'], self.dof, self.np[-1], _ptr(b['z'][-1]), _ptr(b['tgt']),
                                            _ptr(b['dzf'][-1]), _ptr(b['dzh'][-1]),
@@ -352,28 +453,35 @@ class Surrogate:
     def calibrate_steps(self, groups, optimal_iterations=3, quantile=0.75):
         """Fit the step-size proposal on training samples, given as
         ``[(dims, samples), ...]``.  For every sample the RMS errors of the
-        secant predictor (e_s) and of the learned predictor (e_l) against the
-        converged point are measured; ``eps`` is the given quantile of
-        e_l / e_s (how much of the secant error the network removes, read
-        conservatively), ``target`` the median secant error of the steps whose
-        corrector took at most ``optimal_iterations`` iterations (the error a
-        plain step is comfortable with).  Returns the model."""
-        ratios, comfortable, all_es = [], [], []
+        secant predictor (e_s), of the quadratic extrapolation alone (e_q)
+        and of the learned predictor (e_l) against the converged point are
+        measured; ``eps`` is the given quantile of e_l / e_s (how much of the
+        secant error the network removes, read conservatively),
+        ``eps_quadratic`` the same for e_q / e_s, ``target`` the median secant
+        error of the steps whose corrector took at most
+        ``optimal_iterations`` iterations (the error a plain step is
+        comfortable with).  Returns the model."""
+        ratios, qratios, comfortable, all_es = [], [], [], []
         for dims, g in groups:
             for smp in g:
                 smp = self._on_device(smp)
-                xs = smp['x0'] + smp['ds'] * smp['t']
-                xl = self.predict(smp['x0'], smp['t'], smp['mu'], smp['ds'], dims, smp.get('p'))
+                ds, p, phi = smp['ds'], smp.get('p'), smp.get('phi', 0.0)
+                xs = smp['x0'] + ds * smp['t']
+                xq = xs + (ds * ds * phi) * p if (p is not None and phi) else xs
+                xl = self.predict(smp['x0'], smp['t'], smp['mu'], ds, dims, p, phi)
                 es = float((smp['x1'] - xs).pow(2).mean().sqrt())
+                eq = float((smp['x1'] - xq).pow(2).mean().sqrt())
                 el = float((smp['x1'] - xl).pow(2).mean().sqrt())
                 if es > 0:
                     ratios.append(el / es)
+                    qratios.append(eq / es)
                     all_es.append(es)
                     if smp.get('its') is not None and smp['its'] <= optimal_iterations:
                         comfortable.append(es)
         if not ratios:
             raise ValueError('no samples with a nonzero secant error')
         self.step_model = {'eps': float(np.quantile(ratios, quantile)),
+                           'eps_quadratic': float(np.quantile(qratios, quantile)),
                            'target': float(np.median(comfortable if comfortable else all_es))}
         return self.step_model
 
@@ -390,17 +498,20 @@ class Surrogate:
         return ds * min(max(s / abs(ds), 0.5), 2.0)
 
     # -- inference ------------------------------------------------------------------
-    def predict(self, x, t, mu, ds, dims, p=None):
-        """The learned predictor x + ds t + correction (FP64 tensor); p is the
-        previous step's correction per unit step squared (zero if None)."""
+    def predict(self, x, t, mu, ds, dims, p=None, phi=0.0):
+        """The learned predictor x + ds t + ds^2 phi p + correction (FP64
+        tensor); p is the previous step's correction per unit step squared
+        (zero if None) and phi its weight in the quadratic extrapolation for
+        this ds (the phi p term only when the network learns the residual)."""
         if self.scales is None:
             raise RuntimeError('the surrogate has not been trained')
         b = self._buffers(dims)
-        self._pack(b, x, t, mu, ds, p)
+        ps = self._pack(b, x, t, mu, ds, p, phi)
         self._forward(b)
+        xb = self._based(b, x, ds, p, phi)
         xp = torch.empty_like(x)
-        sc = (ctypes.c_double * self.dof)(*[ds * ds * s for s in self.scales['sd']])
-        _lib.check(self.lib.tf_sg_unpack(b['ncell'], self.dof, self.np[-1], _ptr(b['z'][-1]), _ptr(x), _ptr(t),
+        sc = (ctypes.c_double * self.dof)(*self._out_scales(ds, ps))
+        _lib.check(self.lib.tf_sg_unpack(b['ncell'], self.dof, self.np[-1], _ptr(b['z'][-1]), _ptr(xb), _ptr(t),
                                          float(ds), sc, _ptr(xp), _stream()), 'tf_sg_unpack')
         return xp
 
@@ -414,38 +525,76 @@ class LearnedPredictor:
     picks the step (the network then predicts again at that step).  The
     reference picks steps by Newton counts only (Continuation.py:197-209).
     A network whose calibrated error is not below the secant predictor's
-    (eps >= 1) proposes nothing, and steps are proposed only for eps < 1/2."""
+    (eps >= 1) proposes nothing, and steps are proposed only for eps < 1/2.
+
+    Online guard: the network predicts every step, but its prediction is
+    used only when its prediction of the previous step (same step length)
+    was closer to the point the corrector then found than the secant
+    predictor was (the first two steps of a branch, which have no such
+    record, use the secant).  Irregular stretches of a branch -- the first
+    steps from a Stokes state, a fold -- thus fall back to the secant by
+    themselves."""
 
     def __init__(self, surrogate, propose_steps=True):
         self.surrogate = surrogate
         self.propose_steps = propose_steps
+        self.reset()
+
+    def reset(self):
+        """Forget the branch (history, guard and counts): call before the
+        predictor serves another branch."""
         self.calls = 0
         self.steps_proposed = 0
+        self.used = 0
         self._history = _History()
+        self._last = None       # (learned, secant prediction, step) of the previous call
+        self._trust = False
+        # learned / secant error of every judged step (out of sample when the
+        # branch's grid was not trained on)
+        self.ratios = []
 
     # a calibrated network no better than the secant predictor is not used;
     # steps are proposed only by one clearly better
     USE_BELOW = 1.0
     PROPOSE_BELOW = 0.5
 
+    def _judge(self, x0, h):
+        """Compares the previous step's predictions with the point reached."""
+        last, self._last = self._last, None
+        if last is None or h is None:
+            self._trust = False
+            return
+        xl, xs, step = last
+        if step == 0 or abs(h / step - 1.0) > 1e-9:
+            return      # the step was shortened: no comparison
+        el = float((x0 - xl).pow(2).mean().sqrt())
+        es = float((x0 - xs).pow(2).mean().sqrt())
+        if es > 0:
+            self.ratios.append(el / es)
+        self._trust = el < es
+
     def __call__(self, interface, x0, mu0, dx, dmu, ds):
         net = self.surrogate
         if net.scales is None:
             return None
         sm = net.step_model
+        p = self._history.step(dx.data.clone(), float(mu0), dmu) if net.history else None
         if sm is not None and not sm['eps'] < self.USE_BELOW:
-            if net.history:
-                self._history.step(dx.data.clone(), float(mu0), dmu)
             return None
+        self._judge(x0.data, self._history.h)
         self.calls += 1
         dims = (interface.nx, interface.ny, interface.nz)
-        p = self._history.step(dx.data.clone(), float(mu0), dmu) if net.history else None
-        xp = net.predict(x0.data, dx.data, mu0, ds, dims, p)
+        xp = net.predict(x0.data, dx.data, mu0, ds, dims, p, self._history.phi(ds))
+        self._last = (xp, x0.data + ds * dx.data, ds)
+        if not self._trust:
+            return None
+        self.used += 1
         if self.propose_steps and sm is not None and sm['eps'] < self.PROPOSE_BELOW:
             corr = float((xp - x0.data - ds * dx.data).pow(2).mean().sqrt())
             ds_new = net.propose_step(x0.data, dx.data, ds, corr)
             if abs(ds_new / ds - 1.0) > 0.05:
                 self.steps_proposed += 1
-                xp = net.predict(x0.data, dx.data, mu0, ds_new, dims, p)
+                xp = net.predict(x0.data, dx.data, mu0, ds_new, dims, p, self._history.phi(ds_new))
+                self._last = (xp, x0.data + ds_new * dx.data, ds_new)
                 return DeviceVector(xp), mu0 + ds_new * dmu, ds_new
         return DeviceVector(xp), mu0 + ds * dmu
