@@ -217,22 +217,25 @@ def test_gradients_match_cpu_autograd(dims, dof):
     t = torch.randn(ncell * dof, generator=g, dtype=torch.float64).cuda()
     x1 = x + 0.3 * t + 0.01 * torch.randn(ncell * dof, generator=g, dtype=torch.float64).cuda()
     pv = torch.randn(ncell * dof, generator=g, dtype=torch.float64).cuda()
-    sample = {'x0': x, 't': t, 'p': pv, 'mu': 250.0, 'ds': 0.3, 'x1': x1}
+    sample = {'x0': x, 't': t, 'p': pv, 'phi': 0.7, 'mu': 250.0, 'ds': 0.3, 'x1': x1}
     s.fit_scales([sample])
     b = s._buffers(dims)
-    s._pack(b, x, t, sample['mu'], sample['ds'], pv)
-    s._target(b, sample)
+    ps = s._pack(b, x, t, sample['mu'], sample['ds'], pv, sample['phi'])
+    s._target(b, sample, ps)
     s._forward(b)
     s._backward(b, ctypes.c_void_p(b['loss'].data_ptr()), False)
     torch.cuda.synchronize()
     # the packed input, exactly: the scaled state, tangent and previous
-    # correction, then mu and ds
+    # correction (at unit RMS per variable: the residual mode's per-sample
+    # scale), then mu and ds
     x0 = b['x0'].view(ncell, s.kp[0]).float().cpu()
     sc = s.scales
+    rms = pv.view(ncell, dof).pow(2).mean(dim=0).sqrt().cpu() * 0.7
+    assert np.allclose(ps, rms.numpy(), rtol=1e-12)
     want = torch.zeros(ncell, s.kp[0])
     want[:, :dof] = (x.view(ncell, dof).float().cpu() * torch.tensor(sc['sx']).float())
     want[:, dof:2 * dof] = (t.view(ncell, dof).float().cpu() * torch.tensor(sc['st']).float())
-    want[:, 2 * dof:3 * dof] = (pv.view(ncell, dof).float().cpu() * torch.tensor(sc['sp']).float())
+    want[:, 2 * dof:3 * dof] = (pv.view(ncell, dof).float().cpu() * torch.tensor([0.7 / r for r in ps]).float())
     want[:, 3 * dof] = float(np.float32(sample['mu'] * sc['mu']))
     want[:, 3 * dof + 1] = float(np.float32(sample['ds'] * sc['ds']))
     assert torch.equal(x0, ref.bf16(want))
