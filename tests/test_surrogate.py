@@ -151,6 +151,20 @@ def test_quadratic_extrapolation_is_exact_on_a_parabola():
             assert torch.allclose(pred, x(sk + ds), rtol=0, atol=1e-12), (k, ds)
 
 
+def test_step_proposal_from_the_error_ratio():
+    """The proposed step stretches ds by ratio^(-1/3) (the learned error,
+    of third order in the step, then equals the secant error at ds), never
+    shrinks it and at most doubles it; undefined ratios leave ds alone."""
+    from transiflow_gb300.surrogate import Surrogate
+    assert Surrogate.propose_step(100.0, 0.125) == pytest.approx(200.0)
+    assert Surrogate.propose_step(100.0, 0.216) == pytest.approx(100.0 / 0.6)
+    assert Surrogate.propose_step(-50.0, 0.216) == pytest.approx(-50.0 / 0.6)
+    assert Surrogate.propose_step(100.0, 1e-6) == 200.0
+    assert Surrogate.propose_step(100.0, 3.0) == 100.0
+    for bad in (0.0, float('nan'), float('inf'), -1.0):
+        assert Surrogate.propose_step(100.0, bad) == 100.0
+
+
 # -- GPU: the kernels against the oracle ---------------------------------------
 
 def _lib():

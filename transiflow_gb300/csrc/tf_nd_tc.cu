@@ -37,7 +37,12 @@ namespace nd {
 constexpr int TC_BM = 128;
 constexpr int TC_BN = 256;
 constexpr int TC_THREADS = 256;
-constexpr int TC_STAGES = 2;
+// two CTAs per SM, so that one CTA's tensor-core work overlaps the other's
+// gather and epilogue: one stage with split operands (96 KB), two without
+template <int TERMS>
+struct TcStages {
+    static constexpr int n = TERMS == 1 ? 2 : 1;
+};
 constexpr int TC_A_BYTES = TC_BM * 128;                      // 128 rows x 32 FP32
 constexpr int TC_B_BYTES = TC_BN * 128;                      // 256 rows x 32 FP32
 constexpr int TC_EPI_COLS = 128;                             // epilogue pass width
@@ -46,9 +51,9 @@ constexpr int TC_EPI_STRIDE = TC_EPI_COLS + 4;               // floats, conflict
 template <int TERMS>
 struct TcSizes {
     static constexpr int stage = (TERMS == 1 ? 1 : 2) * (TC_A_BYTES + TC_B_BYTES);
-    static constexpr size_t smem = (size_t)TC_STAGES * stage + 1024;   // + alignment slack
+    static constexpr size_t smem = (size_t)TcStages<TERMS>::n * stage + 1024;   // + alignment slack
+    static_assert(TC_BM * TC_EPI_STRIDE * 4 <= TcStages<TERMS>::n * stage, "epilogue staging must fit");
 };
-static_assert(TC_BM * TC_EPI_STRIDE * 4 <= TC_STAGES * (TC_A_BYTES + TC_B_BYTES), "epilogue staging must fit");
 
 // Instruction descriptor of tcgen05.mma .kind::tf32: D FP32 (bits 4-5 = 1),
 // A and B TF32 (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 = 0),
@@ -75,11 +80,12 @@ __device__ __forceinline__ void tc_mma(unsigned tmem, uint64_t adesc, uint64_t b
 }
 
 template <int TERMS>
-__global__ void __launch_bounds__(TC_THREADS, TERMS == 1 ? 2 : 1)
+__global__ void __launch_bounds__(TC_THREADS, 2)
     tc_update_kernel(DevPlan P, int node0, int K0, float *fronts, int32_t *info) {
     constexpr int STAGE = TcSizes<TERMS>::stage;
+    constexpr int TC_STAGES = TcStages<TERMS>::n;
     extern __shared__ unsigned char tc_raw[];
-    __shared__ __align__(8) uint64_t bar[TC_STAGES + 1];
+    __shared__ __align__(8) uint64_t bar[3];
     __shared__ unsigned tmem_slot;
     const int node = node0 + blockIdx.z;
     const int n = P.n_own[node], f = P.f[node];

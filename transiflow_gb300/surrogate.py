@@ -11,8 +11,8 @@ the first, exact tangent h0 = 0).  The network reads the current state
 ``x``, the secant tangent ``t``, ``p``, the parameter ``mu`` and the step
 ``ds`` on the cell grid and proposes what the quadratic still misses; a
 3x3x3 stencil network alone sees only a few cells of what is a global
-curvature, the extrapolation carries it.  Through the predicted correction
-it also proposes the next step size.  The Newton corrector of the
+curvature, the extrapolation carries it.  From its measured accuracy it
+also stretches the next step.  The Newton corrector of the
 continuation judges every point; the secant predictor is the fallback
 whenever the corrector started from the learned predictor does not converge
 within ``Continuation(learned_newton_iterations=4)`` iterations, and
@@ -450,18 +450,16 @@ class Surrogate:
                                            b['lwork'].numel(), _stream()), 'tf_sg_loss')
         return out.cpu().numpy()
 
-    def calibrate_steps(self, groups, optimal_iterations=3, quantile=0.75):
-        """Fit the step-size proposal on training samples, given as
-        ``[(dims, samples), ...]``.  For every sample the RMS errors of the
-        secant predictor (e_s), of the quadratic extrapolation alone (e_q)
-        and of the learned predictor (e_l) against the converged point are
-        measured; ``eps`` is the given quantile of e_l / e_s (how much of the
-        secant error the network removes, read conservatively),
-        ``eps_quadratic`` the same for e_q / e_s, ``target`` the median secant
-        error of the steps whose corrector took at most
-        ``optimal_iterations`` iterations (the error a plain step is
-        comfortable with).  Returns the model."""
-        ratios, qratios, comfortable, all_es = [], [], [], []
+    def calibrate_steps(self, groups, quantile=0.75):
+        """Measures the predictor on samples given as ``[(dims, samples),
+        ...]``: for every sample the RMS errors of the secant predictor
+        (e_s), of the quadratic extrapolation alone (e_q) and of the learned
+        predictor (e_l) against the converged point; ``eps`` is the given
+        quantile of e_l / e_s (how much of the secant error the network
+        removes, read conservatively) and ``eps_quadratic`` the same for
+        e_q / e_s.  A network with eps >= 1 is not used by
+        ``LearnedPredictor``.  Returns the model."""
+        ratios, qratios = [], []
         for dims, g in groups:
             for smp in g:
                 smp = self._on_device(smp)
@@ -475,27 +473,23 @@ class Surrogate:
                 if es > 0:
                     ratios.append(el / es)
                     qratios.append(eq / es)
-                    all_es.append(es)
-                    if smp.get('its') is not None and smp['its'] <= optimal_iterations:
-                        comfortable.append(es)
         if not ratios:
             raise ValueError('no samples with a nonzero secant error')
         self.step_model = {'eps': float(np.quantile(ratios, quantile)),
-                           'eps_quadratic': float(np.quantile(qratios, quantile)),
-                           'target': float(np.median(comfortable if comfortable else all_es))}
+                           'eps_quadratic': float(np.quantile(qratios, quantile))}
         return self.step_model
 
-    def propose_step(self, x, t, ds, correction_rms):
-        """The step at which the learned predictor's expected error, eps *
-        c * ds'^2 with the curvature c = correction_rms / ds^2 the network
-        predicts, equals the comfortable secant error; the ratio to ds stays
-        within [1/2, 2] (the bounds of the Newton-count rule)."""
-        sm = self.step_model
-        if sm is None or correction_rms <= 0 or not math.isfinite(correction_rms):
+    @staticmethod
+    def propose_step(ds, ratio):
+        """The step for a predictor whose error is ``ratio`` times the secant
+        predictor's at ds and of third order in the step (the quadratic
+        extrapolation's order): ds ratio^(-1/3), where its error equals the
+        secant predictor's error at ds -- the step the Newton-count rule
+        chose for the secant predictor -- within [1, 2] times ds (the upper
+        bound of that rule's growth)."""
+        if not ratio > 0 or not math.isfinite(ratio):
             return ds
-        c = correction_rms / (ds * ds)
-        s = math.sqrt(sm['target'] / (sm['eps'] * c))
-        return ds * min(max(s / abs(ds), 0.5), 2.0)
+        return ds * min(max(ratio ** (-1.0 / 3.0), 1.0), 2.0)
 
     # -- inference ------------------------------------------------------------------
     def predict(self, x, t, mu, ds, dims, p=None, phi=0.0):
@@ -518,14 +512,8 @@ class Surrogate:
 
 class LearnedPredictor:
     """The continuation's ``predictor`` hook over a trained surrogate: the
-    state from the network, the parameter from the secant, and -- once
-    ``Surrogate.calibrate_steps`` has run and ``propose_steps`` is set -- the
-    step size: the network's predicted correction of the secant predictor
-    gives the branch's curvature, from which ``Surrogate.propose_step``
-    picks the step (the network then predicts again at that step).  The
-    reference picks steps by Newton counts only (Continuation.py:197-209).
-    A network whose calibrated error is not below the secant predictor's
-    (eps >= 1) proposes nothing, and steps are proposed only for eps < 1/2.
+    state from the network, the parameter from the secant, and -- with
+    ``propose_steps`` -- the step size.
 
     Online guard: the network predicts every step, but its prediction is
     used only when its prediction of the previous step (same step length)
@@ -533,7 +521,15 @@ class LearnedPredictor:
     predictor was (the first two steps of a branch, which have no such
     record, use the secant).  Irregular stretches of a branch -- the first
     steps from a Stokes state, a fold -- thus fall back to the secant by
-    themselves."""
+    themselves.  A network whose calibrated error is not below the secant
+    predictor's (eps >= 1, ``Surrogate.calibrate_steps``) is not used.
+
+    Step size: while the prediction is used, the step the continuation's
+    Newton-count rule chose (for the secant predictor) is stretched by
+    ``Surrogate.propose_step`` from the learned / secant error ratio measured
+    on the last judged step, and the network predicts again at that step.
+    The reference picks steps by Newton counts only (Continuation.py:197-209).
+    """
 
     def __init__(self, surrogate, propose_steps=True):
         self.surrogate = surrogate
@@ -553,10 +549,8 @@ class LearnedPredictor:
         # branch's grid was not trained on)
         self.ratios = []
 
-    # a calibrated network no better than the secant predictor is not used;
-    # steps are proposed only by one clearly better
+    # a calibrated network no better than the secant predictor is not used
     USE_BELOW = 1.0
-    PROPOSE_BELOW = 0.5
 
     def _judge(self, x0, h):
         """Compares the previous step's predictions with the point reached."""
@@ -573,6 +567,12 @@ class LearnedPredictor:
             self.ratios.append(el / es)
         self._trust = el < es
 
+    def _predict(self, x0, dx, mu0, ds, dims, p):
+        xp = self.surrogate.predict(x0.data, dx.data, mu0, ds, dims, p, self._history.phi(ds))
+        # the corrector may update its start in place: judge on a copy
+        self._last = (xp.clone(), x0.data + ds * dx.data, ds)
+        return xp
+
     def __call__(self, interface, x0, mu0, dx, dmu, ds):
         net = self.surrogate
         if net.scales is None:
@@ -584,17 +584,15 @@ class LearnedPredictor:
         self._judge(x0.data, self._history.h)
         self.calls += 1
         dims = (interface.nx, interface.ny, interface.nz)
-        xp = net.predict(x0.data, dx.data, mu0, ds, dims, p, self._history.phi(ds))
-        self._last = (xp, x0.data + ds * dx.data, ds)
+        if self._trust and self.propose_steps and self.ratios:
+            ds_new = net.propose_step(ds, self.ratios[-1])
+            if abs(ds_new / ds - 1.0) > 0.05:
+                self.steps_proposed += 1
+                self.used += 1
+                xp = self._predict(x0, dx, mu0, ds_new, dims, p)
+                return DeviceVector(xp), mu0 + ds_new * dmu, ds_new
+        xp = self._predict(x0, dx, mu0, ds, dims, p)
         if not self._trust:
             return None
         self.used += 1
-        if self.propose_steps and sm is not None and sm['eps'] < self.PROPOSE_BELOW:
-            corr = float((xp - x0.data - ds * dx.data).pow(2).mean().sqrt())
-            ds_new = net.propose_step(x0.data, dx.data, ds, corr)
-            if abs(ds_new / ds - 1.0) > 0.05:
-                self.steps_proposed += 1
-                xp = net.predict(x0.data, dx.data, mu0, ds_new, dims, p, self._history.phi(ds_new))
-                self._last = (xp, x0.data + ds_new * dx.data, ds_new)
-                return DeviceVector(xp), mu0 + ds_new * dmu, ds_new
         return DeviceVector(xp), mu0 + ds * dmu
