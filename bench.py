@@ -475,18 +475,31 @@ def _bandwidth_kernels(itf, reps=4):
                         'frac_hbm': b_spmv / t_spmv / 1e9 / hbm}}
 
 
-# DRAM bytes (read + write) of one launch of the roofline kernel from one ncu
-# capture (see profiles/), keyed by (workload, grid).
+# DRAM bytes (read + write) of the roofline unit -- one FP32 preconditioner
+# application, summed over its apply_kernel launches -- from one ncu capture
+# (profiles/apply_kernel_ldc3d64_application.md), keyed by (nx, nz).
 ROOF_TRAFFIC = {}
 
 
+def application_bytes(plan):
+    """Factor bytes one FP32 application reads: per front the strict lower
+    and the upper own triangle (n^2 in all) and L21 and U12 (2 n (f - n))."""
+    p = plan.host
+    n = p.n_own.astype(np.float64)
+    f = p.f.astype(np.float64)
+    return 4.0 * float(np.sum(n * n + 2.0 * n * (f - n)))
+
+
 def roofline_3d(itf, args):
-    """Live CUDA-event timings at the bench grid.  The roofline kernel is the
-    tensor-core trailing update of the FP32 factorisation (tc_update_kernel):
-    one launch at k0 = 0 over the tree height with the widest fronts, timed
-    alone on the plan's own front buffer (which is scribbled on, so the
-    factorisation is dropped afterwards).  Beside it: the fused assembly, the
-    SpMV, one factorisation and one preconditioner application."""
+    """Live CUDA-event timings at the bench grid.  The roofline unit is the
+    dominant step of the timed branch, one FP32 preconditioner application
+    (apply_kernel, four launches per tree height, replayed from a CUDA
+    graph): HBM-bound, the factor bytes it streams over its event-timed
+    duration.  Beside it: the fused assembly, the SpMV, one factorisation and
+    the tensor-core trailing update (tc_update_kernel) alone -- one launch at
+    k0 = 0 over the tree height with the widest fronts, timed on the plan's
+    own front buffer (which is scribbled on, so the factorisation is dropped
+    afterwards)."""
     import torch
     from transiflow_gb300 import _lib
     from transiflow_gb300.vector import DeviceVector
@@ -533,22 +546,28 @@ def roofline_3d(itf, args):
     tc(0)
     t_tc = _timed(tc, 5)
     solver._owner.pop('fp32', None)       # the fronts no longer hold a factorisation
-    achieved = flops / t_tc / 1e12
-    peak = bf16 / 2.0
-    kernels['tc_update_kernel (alone)'] = {'s_per_launch': t_tc, 'flops': flops, 'TFLOP/s': achieved,
-                                           'front_rw_bytes': c_bytes, 'GB/s': c_bytes / t_tc / 1e9}
-    return {'bound': 'tensor',
-            'kernel': 'tc_update_kernel<%d>: tcgen05 rank-256 trailing update of the FP32 fronts, %dx%dx%d tree '
-                      'height %d (%d fronts), %.1f GFLOP per launch' % (solver.tc_terms, args.nx, args.nx, args.nz,
-                                                                       h, len(nodes), flops / 1e9),
-            'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s', 'frac': achieved / peak,
-            'peak_source': 'TF32 dense rate taken as half the measured BF16 dense rate (%s: MEASURED_PEAKS.json '
-                           'bf16_tflops %.1f); split-TF32 issues %d tensor products per algorithmic one'
-                           % (which, bf16, solver.tc_terms),
-            'traffic': ROOF_TRAFFIC.get(('ldc3d', args.nx, h)),
-            'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (profiles/)',
-            'algorithmic_flops': flops, 'hbm_peak_gbs': hbm, 'hbm_peak_source': '%s (MEASURED_PEAKS.json hbm_gbs)'
-                                                                                 % which,
+    tc_rate = flops / t_tc / 1e12
+    tf32 = bf16 / 2.0
+    kernels['tc_update_kernel (alone)'] = {
+        'what': 'tcgen05 rank-256 trailing update of the FP32 fronts, tree height %d (%d fronts), %.1f GFLOP'
+                % (h, len(nodes), flops / 1e9),
+        's_per_launch': t_tc, 'flops': flops, 'TFLOP/s': tc_rate, 'frac_tf32': tc_rate / tf32,
+        'tf32_peak_source': 'half the measured BF16 dense rate (%s: MEASURED_PEAKS.json bf16_tflops %.1f); '
+                            'split-TF32 issues %d tensor products per algorithmic one' % (which, bf16,
+                                                                                          solver.tc_terms),
+        'front_rw_bytes': c_bytes, 'GB/s': c_bytes / t_tc / 1e9}
+    a_bytes = application_bytes(plan)
+    achieved = a_bytes / t_app / 1e9
+    return {'bound': 'hbm',
+            'kernel': 'one FP32 preconditioner application: apply_kernel<float, 0..3>, four launches per tree '
+                      'height (%d heights), %dx%dx%d, %.2f GB of factors streamed'
+                      % (len(plan.host.levels), args.nx, args.nx, args.nz, a_bytes / 1e9),
+            'achieved': achieved, 'peak': hbm, 'unit': 'GB/s', 'frac': achieved / hbm,
+            'peak_source': '%s (MEASURED_PEAKS.json hbm_gbs, a copy timed alone)' % which,
+            'traffic': ROOF_TRAFFIC.get((args.nx, args.nz)),
+            'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the apply_kernel '
+                              'launches of one application (profiles/apply_kernel_ldc3d64_application.md)',
+            'algorithmic_bytes': a_bytes, 's_per_application': t_app,
             'kernels': kernels}
 
 
