@@ -476,9 +476,13 @@ def _bandwidth_kernels(itf, reps=4):
 
 
 # DRAM bytes (read + write) of the roofline unit -- one FP32 preconditioner
-# application, summed over its apply_kernel launches -- from one ncu capture
-# (profiles/apply_kernel_ldc3d64_application.md), keyed by (nx, nz).
-ROOF_TRAFFIC = {}
+# application, summed over its apply_kernel launches -- keyed by (nx, nz).
+# 64^3 is too large for a multi-metric capture: the ratio of DRAM traffic to
+# algorithmic factor bytes measured over a whole sweep at 32^3 (1.0717:
+# 698.9 MB for 652.3 MB, profiles/apply_kernel_ldc3d32.md) scaled to the
+# 22.951 GB a 64^3 application streams.  Large fronts dominate at 64^3 and
+# have the lowest ratios, so this is an upper estimate.
+ROOF_TRAFFIC = {(64, 64): 1.0717 * 22.951191352e9}
 
 
 def application_bytes(plan):
@@ -565,8 +569,9 @@ def roofline_3d(itf, args):
             'achieved': achieved, 'peak': hbm, 'unit': 'GB/s', 'frac': achieved / hbm,
             'peak_source': '%s (MEASURED_PEAKS.json hbm_gbs, a copy timed alone)' % which,
             'traffic': ROOF_TRAFFIC.get((args.nx, args.nz)),
-            'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the apply_kernel '
-                              'launches of one application (profiles/apply_kernel_ldc3d64_application.md)',
+            'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum over the apply_kernel launches of '
+                              'a backward sweep at 32^3 (1.0717 x its algorithmic bytes), scaled to this '
+                              "application's algorithmic bytes (profiles/apply_kernel_ldc3d32.md)",
             'algorithmic_bytes': a_bytes, 's_per_application': t_app,
             'kernels': kernels}
 
