@@ -27,15 +27,30 @@ def test_direct_solve_matches_reference():
     assert np.linalg.norm(y - g['y']) / np.linalg.norm(g['y']) < 1e-10
 
 
-def test_bordered_solve_matches_reference():
+@pytest.mark.parametrize('method', ['krylov', 'elimination'])
+@pytest.mark.parametrize('precision', ['fp64', 'fp32'])
+def test_bordered_solve_matches_reference(method, precision):
+    """The bordered system [J, V; W^T, C] against the reference's SuperLU
+    solve of its bordered matrix, solved as one FGMRES on the bordered
+    matrix (block preconditioner from the Jacobian's factorisation) or by
+    block elimination.  The single Krylov solve takes about the iterations
+    of one plain solve with the same factorisation."""
     from transiflow_gb300 import Interface
     g = load_golden('solve_ldc2d_12')
-    itf = Interface({'Reynolds Number': float(g['re'])}, 12, 12)
+    itf = Interface({'Reynolds Number': float(g['re']),
+                     'CUDA': {'Bordered Solve': method, 'Factor Precision': precision, 'Tolerance': 1e-12}},
+                    12, 12)
     J = itf.jacobian(itf.vector_from_array(g['state']))
+    st = itf.solver.stats
+    itf.solve(J, itf.vector_from_array(g['b']))
+    plain = st['gmres_iterations']
     y1, y2 = itf.solve(J, itf.vector_from_array(g['b']), float(g['rhs2']), itf.vector_from_array(g['V']),
                        itf.vector_from_array(g['W']), float(g['C']))
+    bordered = st['gmres_iterations'] - plain
     assert np.linalg.norm(y1.numpy() - g['y1']) / np.linalg.norm(g['y1']) < 1e-9
     assert abs(y2 - float(g['y2'])) <= 1e-9 * abs(float(g['y2']))
+    if method == 'krylov':
+        assert bordered <= plain + 2, (plain, bordered)
 
 
 @pytest.mark.parametrize('inverse', [True, False])

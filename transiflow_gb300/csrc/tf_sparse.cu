@@ -185,23 +185,39 @@ __global__ void scan_fixup_kernel(int n, int32_t *a, const int32_t *block_tot) {
 constexpr int RED_THREADS = 256;
 constexpr int RED_BLOCKS = 304;   // 2 x 152 SMs
 
-// partial[b*k + j] = sum over the block's grid-stride chunk of V_j . w
+// partial[b*k + j] = sum over the block's grid-stride chunk of V_j . w.
+// The vectors are taken MD_KV at a time, so w is read once per group of
+// MD_KV vectors (not once per vector); every dot product still adds its
+// terms in the same order, so the result does not depend on the grouping.
+constexpr int MD_KV = 8;
+
 __global__ void __launch_bounds__(RED_THREADS) mdot_partial_kernel(int n, int k, const double *__restrict__ V,
                                                                    long long ldv, const double *__restrict__ w,
                                                                    double *__restrict__ partial) {
-    __shared__ double red[RED_THREADS / 32];
-    for (int j = 0; j < k; ++j) {
-        double acc = 0.0;
-        const double *v = V + (long long)j * ldv;
-        for (int i = blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += gridDim.x * RED_THREADS)
-            acc += __ldg(v + i) * __ldg(w + i);
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __shared__ double red[RED_THREADS / 32][MD_KV];
+    for (int j0 = 0; j0 < k; j0 += MD_KV) {
+        const int kv = min(MD_KV, k - j0);
+        double acc[MD_KV];
+#pragma unroll
+        for (int q = 0; q < MD_KV; ++q) acc[q] = 0.0;
+        const double *v = V + (long long)j0 * ldv;
+        for (int i = blockIdx.x * RED_THREADS + threadIdx.x; i < n; i += gridDim.x * RED_THREADS) {
+            const double wi = __ldg(w + i);
+#pragma unroll
+            for (int q = 0; q < MD_KV; ++q)
+                if (q < kv) acc[q] += __ldg(v + (long long)q * ldv + i) * wi;
+        }
+#pragma unroll
+        for (int q = 0; q < MD_KV; ++q) {
+            double a = acc[q];
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][q] = a;
+        }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double s = 0.0;
-            for (int q = 0; q < RED_THREADS / 32; ++q) s += red[q];
-            partial[blockIdx.x * k + j] = s;
+        if (threadIdx.x < kv) {
+            double sum = 0.0;
+            for (int r = 0; r < RED_THREADS / 32; ++r) sum += red[r][threadIdx.x];
+            partial[blockIdx.x * k + j0 + threadIdx.x] = sum;
         }
         __syncthreads();
     }

@@ -60,6 +60,12 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       after gaining six digits and the next starts from the
                       FP64 residual (iterative refinement), so the solve still
                       meets 'Tolerance' in FP64
+  'Bordered Solve'    'krylov' (default): a bordered system [J, V; W^T, C]
+                      is solved by one FGMRES on the bordered matrix,
+                      preconditioned by the Jacobian's factorisation (block
+                      preconditioner, one application per iteration);
+                      'elimination': block elimination with two solves of
+                      the Jacobian
   'Leaf Cells'        grid cells of a box at which nested dissection stops
                       splitting (default 48)
   'CUDA Graphs'       replay the factorisation and solve launch sequences from
@@ -231,7 +237,8 @@ class Interface(_Base):
                              tc_terms=1 if opts.get('Tensor Core Precision', 'tf32x3') == 'tf32' else 3,
                              storage=opts.get('Factor Storage', 'fp32'),
                              inner=opts.get('Inner Precision', 'fp64'),
-                             equilibrate=opts.get('Equilibrate', True))
+                             equilibrate=opts.get('Equilibrate', True),
+                             bordered=opts.get('Bordered Solve', 'krylov'))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

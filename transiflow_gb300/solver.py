@@ -11,8 +11,12 @@ basis and the update kept in FP64.
 
 Pressure gauge and bordering follow the reference: the right-hand side's
 gauge entry is zeroed (SciPy.py:211-216), and a bordered system
-``[A, sV; sW^T, s^2 C]`` (SciPy.py:51-129) is solved by block elimination
-with two solves of the gauged Jacobian.
+``B = [A, sV; sW^T, s^2 C]`` (SciPy.py:51-129) is solved as one system: FGMRES
+on B with the block preconditioner built from the factorisation M of the
+gauged Jacobian (one application of M per iteration, and one for M sV per
+solve), where the reference factors B itself.  Block elimination with two
+solves of the gauged Jacobian remains available ('Bordered Solve':
+'elimination').
 """
 
 import ctypes
@@ -352,8 +356,14 @@ class Solver:
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
                  reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True, flow=False,
                  flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48, tc_min_front=1024,
-                 tc_terms=3, storage='fp32', inner='fp64', equilibrate=True):
+                 tc_terms=3, storage='fp32', inner='fp64', equilibrate=True, bordered='krylov'):
         self.itf = interface
+        # bordered systems: one FGMRES on the bordered matrix, or block
+        # elimination with two solves of the gauged Jacobian
+        if bordered not in ('krylov', 'elimination'):
+            raise ValueError("'Bordered Solve' must be 'krylov' or 'elimination'")
+        self.bordered = bordered
+        self._bws = None
         # FP32 factorisations: heights whose widest front has at least this
         # many rows use blocked rank-256 tensor-core updates (0: never)
         self.tc_min_front = int(tc_min_front)
@@ -765,9 +775,9 @@ class Solver:
         return self._bordered(op, b, rhs2, V, W, C)
 
     def _bordered(self, op, b, rhs2, V, W, C):
-        """Block elimination of [A_g, sV; sW'^T, s^2 C][y; t] = [b; s rhs2], where
-        W' is W without its gauge entry (SciPy.py:93-126) and b keeps its gauge
-        entry (SciPy.py:226-227)."""
+        """[A_g, sV; sW'^T, s^2 C][y; t] = [b; s rhs2], where W' is W without
+        its gauge entry (SciPy.py:93-126) and b keeps its gauge entry
+        (SciPy.py:226-227)."""
         itf = self.itf
         s = itf.border_scaling
         if np.ndim(rhs2) != 0:
@@ -777,6 +787,9 @@ class Solver:
         if self.gauge >= 0:
             Wt[self.gauge] = 0.0
         Cv = 0.0 if C is None else float(C)
+        if self.bordered == 'krylov':
+            return self._bordered_krylov(op, b, s * float(rhs2), (s * Vt).contiguous(), (s * Wt).contiguous(),
+                                         s * s * Cv, s)
         y0, i0, r0 = self._solve_gauged(op, b.clone())
         y1, i1, r1 = self._solve_gauged(op, (s * Vt).contiguous())
         if max(r0, r1) > max(self.tol, 1e-6):
@@ -787,6 +800,168 @@ class Solver:
         t = (s * float(rhs2) - s * wy0) / (s * s * Cv - s * wy1)
         self._axpby(1.0, y0, -t, y1, y0)
         return DeviceVector(y0), t * s
+
+    # -- the bordered system as one Krylov solve ------------------------------
+    def _bordered_workspace(self, n, dev):
+        m = self.restart
+        if self._bws is None or self._bws['V'].shape[1] != n + 1:
+            lib = _lib.load()
+            wb = lib.tf_vec_mdot_workspace_bytes(n + 1, m + 1)
+            self._bws = {'V': torch.empty((m + 1, n + 1), dtype=torch.float64, device=dev),
+                         'Z': torch.empty((m, n + 1), dtype=torch.float64, device=dev),
+                         'h': torch.empty(m + 2, dtype=torch.float64, device=dev),
+                         'work': torch.empty((wb + 7) // 8, dtype=torch.float64, device=dev),
+                         'q': torch.empty(n, dtype=torch.float64, device=dev),
+                         'r': torch.empty(n + 1, dtype=torch.float64, device=dev),
+                         'x': torch.empty(n + 1, dtype=torch.float64, device=dev)}
+        return self._bws
+
+    def _bdot(self, V, k, w, out):
+        """out[:k] = V[:k] . w over w's length (device)."""
+        lib = _lib.load()
+        ws = self._bws['work']
+        _lib.check(lib.tf_vec_mdot(w.numel(), k, V.data_ptr(), V.stride(0), w.data_ptr(), out.data_ptr(),
+                                   ws.data_ptr(), ws.numel() * 8, _stream()), 'tf_vec_mdot')
+
+    def _bordered_fgmres(self, op, fac, u, w, c, b, beta, maxit):
+        """Flexible GMRES on B = [A_g, u; w^T, c] with the block
+        preconditioner P^-1 [r; rho] = [z - tau q; tau], z = M r, q = M u,
+        tau = (rho - w.z) / (c - w.q): exact when M = A_g^-1, so the
+        iterations are those of one solve with A_g.  Returns (x (n+1),
+        iterations, relative residual)."""
+        n = op.n
+        ws = self._bordered_workspace(n, b.device)
+        V, Z, h, q, r, x = ws['V'], ws['Z'], ws['h'], ws['q'], ws['r'], ws['x']
+        m = self.restart
+        eng = self._engine(fac.precision)
+        lib = _lib.load()
+
+        def prec(src, dst):
+            self._copy(src, eng.vec)
+            eng.solve()
+            self._copy(eng.vec, dst)
+
+        def fill(t, i, v):
+            _lib.check(lib.tf_vec_fill(1, float(v), t.data_ptr() + 8 * i, _stream()), 'tf_vec_fill')
+
+        def scalar(t, i):
+            return float(t[i].item())
+
+        prec(u, q)
+        self._bdot(w.view(1, -1), 1, q, h)
+        delta = c - scalar(h, 0)
+        if delta == 0.0 or not math.isfinite(delta):
+            raise RuntimeError('singular bordered preconditioner')
+        # right-hand side [b; beta]
+        self._copy(b, r[:n])
+        fill(r, n, beta)
+        self._bdot(r.view(1, -1), 1, r, h)
+        bn = math.sqrt(max(scalar(h, 0), 0.0))
+        self._zero(x)
+        if bn == 0.0:
+            return x, 0, 0.0
+        its, relres = 0, 1.0
+        tmp = torch.empty(n, dtype=torch.float64, device=b.device)
+        while its < maxit:
+            self._bdot(r.view(1, -1), 1, r, h)
+            rn = math.sqrt(max(scalar(h, 0), 0.0))
+            relres = rn / bn
+            if relres <= self.tol:
+                break
+            self._axpby(1.0 / rn, r, 0.0, None, V[0])
+            g = [0.0] * (m + 1)
+            g[0] = rn
+            cols, cs, sn = [], [0.0] * m, [0.0] * m
+            k = 0
+            for j in range(m):
+                vj, zj, wv = V[j], Z[j], V[j + 1]
+                rho = scalar(vj, n)
+                prec(vj[:n], zj[:n])
+                self._bdot(w.view(1, -1), 1, zj[:n], h)
+                tau = (rho - scalar(h, 0)) / delta
+                self._axpby(1.0, zj[:n], -tau, q, zj[:n])
+                fill(zj, n, tau)
+                # B z: A_g z_top + tau u; the last row of B P^-1 returns rho
+                op.matvec(zj[:n], wv[:n])
+                self._axpby(1.0, wv[:n], tau, u, wv[:n])
+                fill(wv, n, rho)
+                # classical Gram-Schmidt, twice
+                col = [0.0] * (j + 2)
+                for _ in range(2):
+                    self._bdot(V, j + 1, wv, h)
+                    hj = h[:j + 1]
+                    self._mgs(V, j + 1, hj, wv)
+                    for i, v in enumerate(hj.tolist()):
+                        col[i] += v
+                self._bdot(wv.view(1, -1), 1, wv, h)
+                hn = math.sqrt(max(scalar(h, 0), 0.0))
+                col[j + 1] = hn
+                if hn > 0:
+                    self._axpby(1.0 / hn, wv, 0.0, None, wv)
+                for i in range(j):
+                    t = cs[i] * col[i] + sn[i] * col[i + 1]
+                    col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1]
+                    col[i] = t
+                d = math.hypot(col[j], col[j + 1])
+                cs[j] = col[j] / d if d else 1.0
+                sn[j] = col[j + 1] / d if d else 0.0
+                col[j], col[j + 1] = d, 0.0
+                cols.append(col)
+                g[j + 1] = -sn[j] * g[j]
+                g[j] = cs[j] * g[j]
+                its += 1
+                k = j + 1
+                if abs(g[j + 1]) <= self.tol * bn or its >= maxit or hn == 0:
+                    break
+            R = np.zeros((k, k))
+            for jj in range(k):
+                R[:jj + 1, jj] = cols[jj][:jj + 1]
+            y = np.linalg.solve(R, np.asarray(g[:k]))
+            yd = torch.as_tensor(-y, dtype=torch.float64).to(b.device)
+            self._mgs(Z, k, yd, x)
+            # true residual [b - A_g x_top - x_n u; beta - w.x_top - c x_n]
+            xn = scalar(x, n)
+            op.matvec(x[:n], tmp)
+            self._axpby(1.0, b, -1.0, tmp, r[:n])
+            self._axpby(1.0, r[:n], -xn, u, r[:n])
+            self._bdot(w.view(1, -1), 1, x[:n], h)
+            fill(r, n, beta - scalar(h, 0) - c * xn)
+        self.stats['gmres_iterations'] += its
+        self.stats['last_relres'] = relres
+        if its:
+            self._engine(fac.precision).check()
+        return x, its, relres
+
+    def _bordered_krylov(self, op, b, beta, u, w, c, s):
+        """One FGMRES on the bordered system, preconditioned by the gauged
+        Jacobian's own factorisation, or by the latest one while reusing it
+        is cheaper (as for plain solves); a reuse that does not converge
+        within its iteration budget is redone after a fresh factorisation."""
+        self._count_solve(op)
+        own = op.jac.lu
+        if isinstance(own, Factorization) and own.valid() and own.precision == self.precision:
+            fac, limit = own, self.maxit
+        else:
+            prec = self._prec
+            limit = self._reuse_limit() if self.reuse else 0
+            if (limit >= 2 and prec is not None and prec.valid() and prec.precision == self.precision
+                    and (self.reuse_policy == 'always' or self._drift(op) <= self._drift_tol)):
+                fac = prec
+            else:
+                fac, limit = self.factorize(op), self.maxit
+        x, its, rr = self._bordered_fgmres(op, fac, u, w, c, b, beta, limit)
+        if fac is not op.jac.lu and (not math.isfinite(rr) or rr > self.tol):
+            self.stats['refactored_after_reuse'] += 1
+            self._drift_tol *= 0.5
+            x, its, rr = self._bordered_fgmres(op, self.factorize(op), u, w, c, b, beta, self.maxit)
+        elif fac is not op.jac.lu:
+            self.stats['reused'] += 1
+        if not math.isfinite(rr) or rr > max(self.tol, 1e-6):
+            raise RuntimeError('GMRES did not converge in a bordered solve: relative residual %.3e' % rr)
+        n = op.n
+        y = torch.empty(n, dtype=torch.float64, device=b.device)
+        self._copy(x[:n], y)
+        return DeviceVector(y), float(x[n].item()) * s
 
 
 def _to_tensor(v, device):
