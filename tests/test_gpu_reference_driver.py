@@ -79,7 +79,7 @@ def test_reference_continuation_runs_on_the_cuda_backend(kwargs):
             x0 = cont.newton(itf.vector())
             x, mu = cont.continuation(x0, 'Reynolds Number', 0, 2000, 100,
                                       callback=lambda i, xx, m: pts.append((m, xx.numpy())))
-        runs.append((pts, x.numpy(), mu, itf.calls, itf))
+        runs.append((pts, x.numpy(), mu, list(itf.calls), itf.inner))
     (rp, rx, rmu, rcalls, ritf), (pp, px, pmu, pcalls, _) = runs
     assert abs(rmu - 2000) < 1e-3 and abs(pmu - rmu) <= 1e-9 * abs(rmu)
     assert len(rp) == len(pp) >= 10
