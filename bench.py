@@ -913,29 +913,43 @@ def batched(args):
     """The batched configuration: many independent lid-driven cavities of
     uneven size and Reynolds number, each by Newton at Re = 0 and continuation
     to its Re with ||F|| <= 1e-10, solved concurrently (one stream per
-    instance) and one after the other on the same GPU."""
+    instance) and one after the other on the same GPU.  Under torchrun the
+    instances are sharded over the ranks (one GPU each, largest first to the
+    least loaded rank) and the results gathered on every rank; the time is
+    the slowest rank's."""
     import torch
-    from transiflow_gb300.batch import solve_instance, solve_many
-    rng = np.random.default_rng(2)
-    specs = [{'nx': int(rng.choice(np.arange(32, 193, 16))), 'target': float(rng.uniform(100, 4000)),
-              'ds': 200.0, 'tolerance': 1e-10} for _ in range(args.batched)]
-    solve_many(specs[:4])                      # plans and kernels warm
-    for sp in {s['nx']: s for s in specs}.values():
-        solve_instance(dict(sp, target=100.0))  # every grid shape's plan built before timing
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    res = solve_many(specs)
-    torch.cuda.synchronize()
-    t_conc = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    for sp in specs:
-        solve_instance(sp)
-    torch.cuda.synchronize()
-    t_seq = time.perf_counter() - t0
-    print(json.dumps({'batched': args.batched, 'concurrent_s': t_conc, 'sequential_s': t_seq,
-                      'max_fnorm': max(r['fnorm'] for r in res),
-                      'unknowns': int(sum(3 * s['nx'] ** 2 for s in specs))}))
-
+    from transiflow_gb300 import dist
+    from transiflow_gb300.batch import shard, solve_instance, solve_many, solve_sharded
+    rank, world, local = dist.init_from_env()
+    torch.cuda.set_device(local)
+    try:
+        rng = np.random.default_rng(2)
+        specs = [{'nx': int(rng.choice(np.arange(32, 193, 16))), 'target': float(rng.uniform(100, 4000)),
+                  'ds': 200.0, 'tolerance': 1e-10} for _ in range(args.batched)]
+        mine = [specs[i] for i in shard(specs, world, rank)]
+        solve_many(mine[:4])                       # plans and kernels warm
+        for sp in {s['nx']: s for s in mine}.values():
+            solve_instance(dict(sp, target=100.0))  # every grid shape's plan built before timing
+        torch.cuda.synchronize()
+        dist.barrier()
+        t0 = time.perf_counter()
+        res = solve_sharded(specs)
+        torch.cuda.synchronize()
+        t_conc = dist.max_over_ranks(time.perf_counter() - t0)
+        out = {'batched': args.batched, 'n_gpus': world, 'concurrent_s': t_conc,
+               'instances_per_rank': [len(shard(specs, world, r)) for r in range(world)],
+               'max_fnorm': max(r['fnorm'] for r in res),
+               'unknowns': int(sum(3 * s['nx'] ** 2 for s in specs))}
+        if world == 1:
+            t0 = time.perf_counter()
+            for sp in specs:
+                solve_instance(sp)
+            torch.cuda.synchronize()
+            out['sequential_s'] = time.perf_counter() - t0
+        if rank == 0:
+            print(json.dumps(out))
+    finally:
+        dist.finalize()
 
 
 def main():

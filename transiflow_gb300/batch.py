@@ -12,13 +12,19 @@ most SMs idle on their own, overlap on the GPU; every libtfcuda call is
 stream-ordered and the host synchronisations of one instance wait only for
 its own stream.  Elimination plans are shared between instances of the same
 grid shape.
+
+Across GPUs the instances are sharded, not replicated: ``shard`` assigns
+each instance to one rank (largest estimated cost first, to the least loaded
+rank; the same on every rank, no communication), ``solve_sharded`` solves a
+rank's share with ``solve_many`` and gathers every result on every rank in
+the order of the specs -- the only exchange between ranks.
 """
 
 import threading
 
 import torch
 
-from . import _lib
+from . import _lib, dist
 
 from .continuation import Continuation
 from .interface import Interface
@@ -84,3 +90,58 @@ def solve_many(specs, concurrency=None):
         if e is not None:
             raise e
     return results
+
+
+def instance_cost(spec):
+    """Relative cost estimate of one instance: the multifrontal solve of a
+    grid with N unknowns scales like N^1.5 in 2D and N^2 in 3D, times the
+    continuation steps to the target (about target / ds, at least one)."""
+    nx = int(spec['nx'])
+    ny = int(spec.get('ny', nx))
+    nz = int(spec.get('nz', 1))
+    cells = nx * ny * nz
+    work = cells ** (2.0 if nz > 1 else 1.5)
+    steps = 1.0 + abs(float(spec['target']) - float(spec.get('start', 0.0))) / float(spec.get('ds', 100.0))
+    return work * steps
+
+
+def shard(specs, world, rank):
+    """Indices (ascending) of the instances rank ``rank`` of ``world`` solves.
+    Longest estimated cost first, each to the currently least loaded rank
+    (ties: the lower rank); deterministic, so every rank computes the same
+    partition without communicating."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError('rank %d outside a world of %d' % (rank, world))
+    costs = [instance_cost(sp) for sp in specs]
+    load = [0.0] * world
+    owner = [0] * len(specs)
+    for i in sorted(range(len(specs)), key=lambda i: (-costs[i], i)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[i] = r
+        load[r] += costs[i]
+    return [i for i in range(len(specs)) if owner[i] == rank]
+
+
+def solve_sharded(specs, concurrency=None, solver=None):
+    """Solve ``specs`` across the ranks of the initialised process group
+    (one GPU each): every rank solves its shard concurrently on its GPU
+    (``solve_many``, or ``solver`` -- a callable taking a list of specs and
+    returning their results), then all results are gathered on every rank
+    in the order of ``specs``.  Without a process group this is
+    ``solve_many``."""
+    import torch.distributed as tdist
+    specs = list(specs)
+    solver = solver or (lambda sp: solve_many(sp, concurrency))
+    if not tdist.is_initialized():
+        return solver(specs)
+    world, rank = tdist.get_world_size(), tdist.get_rank()
+    mine = shard(specs, world, rank)
+    local = solver([specs[i] for i in mine]) if mine else []
+    parts = [None] * world
+    tdist.all_gather_object(parts, list(zip(mine, local)))
+    out = [None] * len(specs)
+    for part in parts:
+        for i, res in part:
+            out[i] = res
+    dist.barrier()
+    return out
