@@ -327,8 +327,11 @@ int tf_nd_factor_inv_f32(const tf_nd_plan *plan, const double *d_vals, float *d_
                          tf_stream_t aux_stream);
 /* In-place solve with inverted own blocks (after tf_nd_invert_*): d_x as in
  * tf_nd_solve_*; d_scratch: tf_nd_solve_inv_workspace_bytes(plan) bytes of
- * device scratch (one value per front index entry; the query reads the
- * plan's last index offset from the device, a synchronising copy).         */
+ * device scratch, the larger of one double per front index entry (FP64
+ * factors) and 2 n doubles (FP32 / BF16 factors: the vectors y and z of the
+ * application, addressed by unknown); the query reads the plan's last index
+ * offset from the device, a synchronising copy.  Replaces SuperLU's solve
+ * in SciPy.Interface.direct_solve (transiflow/interface/SciPy.py:204-258). */
 size_t tf_nd_solve_inv_workspace_bytes(const tf_nd_plan *plan);
 int tf_nd_solve_inv_f64(const tf_nd_plan *plan, const double *d_fronts, const int32_t *d_piv,
                         double *d_x, double *d_scratch, tf_stream_t stream);
