@@ -77,10 +77,8 @@ def parse():
     ap.add_argument('--train-grids', default='32,48', help='training grid sizes (cubes)')
     ap.add_argument('--train-seeds', default='3,4,5,6', help='one training branch per seed and grid')
     ap.add_argument('--train-target', type=float, default=2500.0, help='Re at the end of the training branches')
-    ap.add_argument('--train-ds', type=float, default=1000.0,
-                    help='training branches: largest step (the first is drawn from [0.8, 1.2] x --ds); the '
-                         "default is the continuation's own limit, so the training steps follow the step rule "
-                         'of the timed branch')
+    ap.add_argument('--train-ds', type=float, default=50.0,
+                    help='training branches: largest step (the first is drawn from [0.8, 1.2] x --ds)')
     ap.add_argument('--train-tol', type=float, default=1e-7, help='training branches: Newton tolerance on ||F||')
     ap.add_argument('--train-steps', type=int, default=150, help='Adam steps per grid and round')
     ap.add_argument('--train-rounds', type=int, default=4, help='rounds over the training grids')
@@ -253,10 +251,10 @@ def train_predictor(args):
             x0 = cont.newton(itf.vector(), args.train_tol)
             # first step near the bench's own (a first step of a few tens from
             # Re = 0 lands where the reference's Re = 0 -> 1 viscosity
-            # substitution makes the secant tangent useless), later steps by
-            # the Newton-count rule up to --train-ds: a network trained on
-            # much shorter steps than the timed branch takes did not carry
-            # over to it
+            # substitution makes the secant tangent useless), later steps at
+            # most --train-ds so that the branch yields many regular points
+            # (with the timed branch's own step rule, up to 1000, the 32^3 and
+            # 48^3 branches left 15 steps the three-point history describes)
             ds = args.ds * float(np.random.default_rng(seed).uniform(0.8, 1.2))
             try:
                 cont.continuation(x0, 'Reynolds Number', 0.0, args.train_target, ds, ds_max=args.train_ds)
@@ -273,7 +271,7 @@ def train_predictor(args):
             # three-point history does not describe are dropped by
             # regular_steps
             kept = regular_steps([smp for smp in rec.samples
-                                  if smp['ds'] >= 0.25 * args.ds and (smp['its'] or 0) >= 1])
+                                  if smp['ds'] >= 0.25 * args.train_ds and (smp['its'] or 0) >= 1])
             dropped += len(rec.samples) - len(kept)
             groups.append(((n, n, n), kept))
             del itf, cont, x0

@@ -517,9 +517,9 @@ class LearnedPredictor:
 
     Online guard: the network predicts every step, but its prediction is
     used only when its prediction of the previous step (same step length)
-    was closer to the point the corrector then found than the secant
-    predictor was (the first two steps of a branch, which have no such
-    record, use the secant).  Irregular stretches of a branch -- the first
+    was clearly closer to the point the corrector then found than the secant
+    predictor was (error below TRUST_BELOW = 0.8 of the secant's; the first
+    two steps of a branch, which have no such record, use the secant).  Irregular stretches of a branch -- the first
     steps from a Stokes state, a fold -- thus fall back to the secant by
     themselves.  A network whose calibrated error is not below the secant
     predictor's (eps >= 1, ``Surrogate.calibrate_steps``) is not used.
@@ -551,6 +551,10 @@ class LearnedPredictor:
 
     # a calibrated network no better than the secant predictor is not used
     USE_BELOW = 1.0
+    # the prediction is used while its last judged error was below this
+    # fraction of the secant predictor's: one barely better does not pay for
+    # the corrector iterations a rejected prediction costs
+    TRUST_BELOW = 0.8
 
     def _judge(self, x0, h):
         """Compares the previous step's predictions with the point reached."""
@@ -565,7 +569,7 @@ class LearnedPredictor:
         es = float((x0 - xs).pow(2).mean().sqrt())
         if es > 0:
             self.ratios.append(el / es)
-        self._trust = el < es
+        self._trust = el < self.TRUST_BELOW * es
 
     def _predict(self, x0, dx, mu0, ds, dims, p):
         xp = self.surrogate.predict(x0.data, dx.data, mu0, ds, dims, p, self._history.phi(ds))
