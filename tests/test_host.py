@@ -110,6 +110,27 @@ def test_c_abi_exports_every_declared_symbol(built_lib):
         assert ctypes.cast(getattr(built_lib, name), ctypes.c_void_p).value
 
 
+def test_plan_with_too_many_fronts_in_a_height_is_refused(built_lib):
+    """A height with more fronts than a grid dimension holds (65535) makes
+    every per-height entry point return TF_ERR_SIZE before any CUDA call (so
+    this runs without a GPU; the device pointers are never read)."""
+    from transiflow_gb300 import _lib
+    fake = ctypes.c_void_p(16)
+    level_ptr = (ctypes.c_int32 * 3)(0, 1, 70002)
+    sizes = (ctypes.c_int32 * 2)(4, 8)
+    p = _lib.NdPlan()
+    p.n, p.nnodes, p.nlevels = 4 * 70002, 70002, 2
+    p.level_ptr = ctypes.cast(level_ptr, ctypes.c_void_p)
+    p.max_own = p.max_f = ctypes.cast(sizes, ctypes.c_void_p)
+    for f in ('d_n_own', 'd_f', 'd_parent', 'd_front_off', 'd_idx_off', 'd_idx', 'd_ea_off', 'd_ea_map',
+              'd_scat_pos', 'd_scat_src', 'd_piv_off', 'd_rank'):
+        setattr(p, f, fake)
+    fn = built_lib.tf_nd_solve_inv_f32
+    fn.argtypes = [ctypes.c_void_p] * 6
+    fn.restype = ctypes.c_int
+    assert fn(ctypes.cast(ctypes.pointer(p), ctypes.c_void_p), fake, fake, fake, fake, None) == 4
+
+
 def test_python_binding_matches_the_header():
     """Every entry point the ctypes binding declares is in the header with
     the same number of parameters and a matching return type (the binding

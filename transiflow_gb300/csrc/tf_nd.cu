@@ -493,6 +493,10 @@ int check_plan(const tf_nd_plan *p) {
     if (!p->d_n_own || !p->d_f || !p->d_parent || !p->d_front_off || !p->d_idx_off || !p->d_idx ||
         !p->d_ea_off || !p->d_ea_map || !p->d_scat_pos || !p->d_scat_src || !p->d_piv_off || !p->d_rank)
         return TF_ERR_ARG;
+    // the per-height launches put a height's fronts on a grid dimension
+    // whose limit is 65535 (at 64^3 the widest height has 4097 fronts)
+    for (int h = 0; h < p->nlevels; ++h)
+        if (p->level_ptr[h + 1] - p->level_ptr[h] > 65535) return TF_ERR_SIZE;
     return TF_OK;
 }
 
