@@ -9,23 +9,45 @@
 namespace tf {
 
 // ---------------------------------------------------------------------------
-// SpMV: 8 lanes per row (rows hold 4..19 entries), coalesced within a group
+// SpMV on the stencil CSR (rows hold 4..19 entries)
 // ---------------------------------------------------------------------------
+// SpMV with one lane per row: a warp takes 32 consecutive rows, stages their
+// entries (contiguous in the CSR) in shared memory with coalesced loads, and
+// every lane then sums its own row serially -- one FP64 FMA per entry and no
+// shuffle sums.  (Eight lanes per row with a shuffle sum, the earlier
+// design, spent more FP64 issue slots on the sums than on the products:
+// GB300 issues two FP64 FMAs per SM and cycle.)
+constexpr int SPR_WARPS = 4;
+constexpr int SPR_CHUNK = 32 * 24;       // entries of a warp staged at once
+
 template <typename TV>
-__global__ void __launch_bounds__(256) spmv_kernel(int n, const int32_t *__restrict__ rowptr,
-                                                   const int32_t *__restrict__ cols,
-                                                   const TV *__restrict__ vals, const double *__restrict__ x,
-                                                   double *__restrict__ y, double alpha, double beta) {
-    const int lane = threadIdx.x & 7;
-    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
-    if (row >= n) return;
-    const int b = __ldg(rowptr + row), e = __ldg(rowptr + row + 1);
+__global__ void __launch_bounds__(32 * SPR_WARPS) spmv_rows_kernel(int n, const int32_t *__restrict__ rowptr,
+                                                                   const int32_t *__restrict__ cols,
+                                                                   const TV *__restrict__ vals,
+                                                                   const double *__restrict__ x,
+                                                                   double *__restrict__ y, double alpha,
+                                                                   double beta) {
+    __shared__ TV sv[SPR_WARPS][SPR_CHUNK];
+    __shared__ int32_t sc[SPR_WARPS][SPR_CHUNK];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r0 = (blockIdx.x * SPR_WARPS + warp) * 32;
+    if (r0 >= n) return;
+    const int row = r0 + lane;
+    const int base = __ldg(rowptr + r0), end = __ldg(rowptr + min(n, r0 + 32));
+    const int b = row < n ? __ldg(rowptr + row) : end, e = row < n ? __ldg(rowptr + row + 1) : end;
     double acc = 0.0;
-    for (int t = b + lane; t < e; t += 8) acc += (double)__ldg(vals + t) * __ldg(x + __ldg(cols + t));
-    acc += __shfl_down_sync(0xffffffffu, acc, 4, 8);
-    acc += __shfl_down_sync(0xffffffffu, acc, 2, 8);
-    acc += __shfl_down_sync(0xffffffffu, acc, 1, 8);
-    if (lane == 0) y[row] = beta == 0.0 ? alpha * acc : alpha * acc + beta * y[row];
+    for (int c0 = base; c0 < end; c0 += SPR_CHUNK) {
+        const int c1 = min(end, c0 + SPR_CHUNK);
+        for (int t = c0 + lane; t < c1; t += 32) {
+            sv[warp][t - c0] = __ldg(vals + t);
+            sc[warp][t - c0] = __ldg(cols + t);
+        }
+        __syncwarp();
+        const int lo = max(b, c0), hi = min(e, c1);
+        for (int t = lo; t < hi; ++t) acc += (double)sv[warp][t - c0] * __ldg(x + sc[warp][t - c0]);
+        __syncwarp();
+    }
+    if (row < n) y[row] = beta == 0.0 ? alpha * acc : alpha * acc + beta * y[row];
 }
 
 // Copy with row g and column g replaced by a single -1 on the diagonal
@@ -314,7 +336,7 @@ extern "C" int tf_gauge_values(int n, const int32_t *d_rowptr, const int32_t *d_
 extern "C" int tf_spmv_f64(int n, const int32_t *d_rowptr, const int32_t *d_cols, const double *d_vals,
                            const double *d_x, double *d_y, double alpha, double beta, tf_stream_t stream) {
     if (n <= 0 || !d_rowptr || !d_cols || !d_vals || !d_x || !d_y) return TF_ERR_ARG;
-    spmv_kernel<double><<<blocks_for((long long)n * 8, 256), 256, 0, (cudaStream_t)stream>>>(
+    spmv_rows_kernel<double><<<blocks_for((long long)n, 32 * SPR_WARPS), 32 * SPR_WARPS, 0, (cudaStream_t)stream>>>(
         n, d_rowptr, d_cols, d_vals, d_x, d_y, alpha, beta); launched();
     return cuda_status();
 }
@@ -322,7 +344,7 @@ extern "C" int tf_spmv_f64(int n, const int32_t *d_rowptr, const int32_t *d_cols
 extern "C" int tf_spmv_f32(int n, const int32_t *d_rowptr, const int32_t *d_cols, const float *d_vals,
                            const double *d_x, double *d_y, double alpha, double beta, tf_stream_t stream) {
     if (n <= 0 || !d_rowptr || !d_cols || !d_vals || !d_x || !d_y) return TF_ERR_ARG;
-    spmv_kernel<float><<<blocks_for((long long)n * 8, 256), 256, 0, (cudaStream_t)stream>>>(
+    spmv_rows_kernel<float><<<blocks_for((long long)n, 32 * SPR_WARPS), 32 * SPR_WARPS, 0, (cudaStream_t)stream>>>(
         n, d_rowptr, d_cols, d_vals, d_x, d_y, alpha, beta); launched();
     return cuda_status();
 }
