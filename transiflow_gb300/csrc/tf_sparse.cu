@@ -44,6 +44,8 @@ __global__ void __launch_bounds__(32 * SPR_WARPS) spmv_rows_kernel(int n, const 
         }
         __syncwarp();
         const int lo = max(b, c0), hi = min(e, c1);
+        // unrolled so that several gathers of x are in flight per lane
+#pragma unroll 4
         for (int t = lo; t < hi; ++t) acc += (double)sv[warp][t - c0] * __ldg(x + sc[warp][t - c0]);
         __syncwarp();
     }
