@@ -908,6 +908,9 @@ def profile_stage(args):
     if plan is not None:
         out.update({'first_factor_s': first, 'factor_gflop': plan.flops / 1e9,
                     'front_gb': plan.front_elems * (8 if args.precision == 'fp64' else 4) / 1e9})
+        eng = itf.solver._engines.get(args.precision)
+        if eng is not None:
+            out['apply_waves'] = int(eng.struct.apply_waves)
     print(json.dumps(out))
 
 

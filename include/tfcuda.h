@@ -275,6 +275,11 @@ typedef struct tf_nd_plan {
      * other value) = operands split into TF32 high parts and remainders,
      * three products per term, close to FP32 accuracy                        */
     int32_t tc_terms;
+    /* FP32 / BF16 applications: warps per SM a height's launch aims for
+     * before a warp takes fewer column tiles (0: 64).  Tuned at run time by
+     * the Python solver ('Tune Application'); any value gives the same
+     * results up to the order of the atomic sums.                          */
+    int32_t apply_waves;
 } tf_nd_plan;
 
 /* Numeric factorisation of the (gauged) stencil-CSR values.  d_fronts holds

@@ -249,3 +249,27 @@ def test_fp32_inner_products_with_fp64_refinement(shape, params):
         assert np.linalg.norm(A @ y - bg) / np.linalg.norm(bg) < 1e-11
         ys.append(y)
     assert np.linalg.norm(ys[1] - ys[0]) / np.linalg.norm(ys[0]) < 1e-9
+
+
+def test_tuned_application_solves_the_same_system(tmp_path, monkeypatch):
+    """With 'Tune Application' the first FP32 factorisation times the
+    application's launch shapes and keeps the fastest (cached per GPU, grid
+    and precision); the solve agrees with the untuned one to the solver
+    tolerance, and a second interface on the same grid reads the cache."""
+    from transiflow_gb300 import Interface, solver
+    monkeypatch.setattr(solver, '_TUNE_CACHE', solver.TuneCache(str(tmp_path / 'tune.json')))
+    n = 10 * 10 * 8 * 4
+    x0 = 0.5 * np.random.default_rng(3).standard_normal(n)
+    b = np.random.default_rng(5).standard_normal(n)
+    ys, waves = [], []
+    for tune in (False, True, True):
+        itf = Interface({'Reynolds Number': 300,
+                         'CUDA': {'Factor Precision': 'fp32', 'Tolerance': 1e-12, 'Tune Application': tune}},
+                        10, 10, 8)
+        J = itf.jacobian(itf.vector_from_array(x0))
+        ys.append(itf.solve(J, itf.vector_from_array(b)).numpy())
+        waves.append(itf.solver._engine('fp32').struct.apply_waves)
+    assert waves[0] == 0 and waves[1] in solver.APPLY_WAVES and waves[2] == waves[1]
+    assert solver._TUNE_CACHE.get(itf.solver._tune_key('fp32')) == waves[1]
+    for y in ys[1:]:
+        assert np.linalg.norm(y - ys[0]) <= 1e-9 * np.linalg.norm(ys[0])

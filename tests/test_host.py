@@ -344,3 +344,22 @@ def test_parameter_files_round_trip(tmp_path):
     assert back['Shift'] == 1 + 2j
     assert back['Profile'] == [0.0, 1.0, 2.0]
     assert back['Problem Type'] == 'Lid-driven Cavity' and back['Grid Stretching Factor'] == 1.5
+
+
+def test_tuner_picks_the_fastest_median_and_caches_it(tmp_path):
+    """The application tuner's selection (median of repeated timings, ties to
+    the earlier candidate) and its JSON cache: entries survive a new cache
+    object on the same file, and an unreadable file only means no entries."""
+    from transiflow_gb300.solver import APPLY_WAVES, TuneCache, pick_fastest
+    times = {16: [3.0, 1.0, 3.0], 32: [2.0, 2.0, 9.0], 64: [2.0, 2.0, 2.0], 128: [5.0, 5.0, 5.0]}
+    calls = {k: iter(v) for k, v in times.items()}
+    assert pick_fastest(APPLY_WAVES, lambda c: next(calls[c])) == 32
+    path = str(tmp_path / 'sub' / 'tune.json')
+    c = TuneCache(path)
+    assert c.get('k') is None
+    c.put('k', 64)
+    c.put('other', 16)
+    assert TuneCache(path).get('k') == 64 and TuneCache(path).get('other') == 16
+    with open(path, 'w') as f:
+        f.write('{not json')
+    assert TuneCache(path).get('k') is None

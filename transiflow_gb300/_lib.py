@@ -95,7 +95,7 @@ class NdPlan(ctypes.Structure):
                 ('nscat', ctypes.c_int64), ('d_scat_pos', ctypes.c_void_p), ('d_scat_src', ctypes.c_void_p),
                 ('scat_level_ptr', ctypes.c_void_p), ('d_piv_off', ctypes.c_void_p),
                 ('d_rank', ctypes.c_void_p), ('front_elems', ctypes.c_int64), ('tc_min_front', ctypes.c_int32),
-                ('tc_terms', ctypes.c_int32)]
+                ('tc_terms', ctypes.c_int32), ('apply_waves', ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p

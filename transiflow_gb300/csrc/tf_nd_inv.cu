@@ -836,14 +836,16 @@ static int inv_bnd(const DevPlan &D, int node0, int cnt, int rows, int cols, int
 
 // One product of the FP32 / BF16 application over every front of a height
 // (at most `rows` rows and `cols` columns per front).  A warp takes up to ACT
-// column tiles; fewer when the height would otherwise give the GPU fewer than
-// about four waves of warps.
+// column tiles; fewer when the height would otherwise give the GPU fewer
+// than `waves` warps per SM (the plan's apply_waves, 64 by default: about
+// four waves of the 16-20 warps an SM holds).
 template <typename S, int KIND>
-static int apply_launch(const DevPlan &D, int node0, int cnt, int rows, int cols, int nsm, const S *fronts,
-                        const int32_t *piv, const double *vin, double *vout, bool pdl, cudaStream_t s) {
+static int apply_launch(const DevPlan &D, int node0, int cnt, int rows, int cols, int nsm, int waves,
+                        const S *fronts, const int32_t *piv, const double *vin, double *vout, bool pdl,
+                        cudaStream_t s) {
     if (rows <= 0 || cols <= 0) return TF_OK;
     constexpr bool TRI = KIND == AP_FTRI || KIND == AP_BTRI;
-    const int64_t target = 64 * (int64_t)nsm;
+    const int64_t target = (int64_t)waves * nsm;
     int ct = ACT;
     for (; ct > 1; ct /= 2) {
         int64_t warps = (int64_t)((rows + AR - 1) / AR) * cnt * ((cols + ct * SB - 1) / (ct * SB));
@@ -898,6 +900,7 @@ static int solve_inv(const tf_nd_plan *p, const DevPlan &D, const T *fronts, con
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
             return TF_ERR_CUDA;
         const size_t n = (size_t)p->n;
+        const int waves = p->apply_waves > 0 ? p->apply_waves : 64;
         double *y = scratch, *z = scratch + n;
         if (cudaMemsetAsync(scratch, 0, 2 * n * sizeof(double), s) != cudaSuccess) return TF_ERR_CUDA;
         bool first = true;   // the first launch waits for the memset
@@ -906,17 +909,21 @@ static int solve_inv(const tf_nd_plan *p, const DevPlan &D, const T *fronts, con
             const int mo = p->max_own[h], mf = p->max_f[h];
             if (cnt <= 0 || mo <= 0) continue;
             const int nb = cnt == 1 ? mf - mo : mf;     // boundary rows of a front, at most
-            if ((e = apply_launch<T, AP_FTRI>(D, node0, cnt, mo, mo, nsm, fronts, piv, x, y, !first, s))) return e;
+            if ((e = apply_launch<T, AP_FTRI>(D, node0, cnt, mo, mo, nsm, waves, fronts, piv, x, y, !first, s)))
+                return e;
             first = false;
-            if ((e = apply_launch<T, AP_FBND>(D, node0, cnt, nb, mo, nsm, fronts, piv, y, x, true, s))) return e;
+            if ((e = apply_launch<T, AP_FBND>(D, node0, cnt, nb, mo, nsm, waves, fronts, piv, y, x, true, s)))
+                return e;
         }
         for (int h = p->nlevels - 1; h >= 0; --h) {
             const int node0 = p->level_ptr[h], cnt = p->level_ptr[h + 1] - node0;
             const int mo = p->max_own[h], mf = p->max_f[h];
             if (cnt <= 0 || mo <= 0) continue;
             const int nb = cnt == 1 ? mf - mo : mf;
-            if ((e = apply_launch<T, AP_BBND>(D, node0, cnt, mo, nb, nsm, fronts, piv, z, y, true, s))) return e;
-            if ((e = apply_launch<T, AP_BTRI>(D, node0, cnt, mo, mo, nsm, fronts, piv, y, z, true, s))) return e;
+            if ((e = apply_launch<T, AP_BBND>(D, node0, cnt, mo, nb, nsm, waves, fronts, piv, z, y, true, s)))
+                return e;
+            if ((e = apply_launch<T, AP_BTRI>(D, node0, cnt, mo, mo, nsm, waves, fronts, piv, y, z, true, s)))
+                return e;
         }
         if (cudaMemcpyAsync(x, z, n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
             return TF_ERR_CUDA;

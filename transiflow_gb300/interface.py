@@ -66,6 +66,11 @@ Backend options go in the ``'CUDA'`` sub-dictionary of the parameters:
                       preconditioner, one application per iteration);
                       'elimination': block elimination with two solves of
                       the Jacobian
+  'Tune Application'  FP32 / BF16 factors: time the application's launch
+                      shapes (warps per SM a height aims for) on the first
+                      factorisation and keep the fastest, cached per GPU,
+                      grid and precision in TRANSIFLOW_GB300_TUNE_CACHE or
+                      ~/.cache/transiflow_gb300/tune.json (default True)
   'Leaf Cells'        grid cells of a box at which nested dissection stops
                       splitting (default 48)
   'CUDA Graphs'       replay the factorisation and solve launch sequences from
@@ -238,7 +243,8 @@ class Interface(_Base):
                              storage=opts.get('Factor Storage', 'fp32'),
                              inner=opts.get('Inner Precision', 'fp64'),
                              equilibrate=opts.get('Equilibrate', True),
-                             bordered=opts.get('Bordered Solve', 'krylov'))
+                             bordered=opts.get('Bordered Solve', 'krylov'),
+                             tune=opts.get('Tune Application', True))
         self.fuse = opts.get('Fuse Jacobian', False)
         self._cached_jac = None
         self.calls = {'rhs': 0, 'jacobian': 0, 'solve': 0, 'fused_jacobians': 0}

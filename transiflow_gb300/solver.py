@@ -20,7 +20,9 @@ solves of the gauged Jacobian remains available ('Bordered Solve':
 """
 
 import ctypes
+import json
 import math
+import os
 import threading
 
 import numpy as np
@@ -195,6 +197,8 @@ class Factorization:
         eng = solver._engine(precision)
         solver._copy(op.values, eng.staging)
         eng.factor()
+        if solver.tune and not eng.tuned:
+            eng.tune(solver._tune_key(precision), _TUNE_CACHE)
 
     def valid(self):
         return self.solver._owner.get(self.precision) is self
@@ -205,6 +209,67 @@ class Factorization:
         self.solver._copy(x, eng.vec)
         eng.solve()
         self.solver._copy(eng.vec, x)
+
+
+# -- run-time tuning of the application's launch shape -----------------------
+# Warps per SM a height's FP32 / BF16 application launch aims for before its
+# warps take fewer column tiles (the plan's apply_waves).
+APPLY_WAVES = (16, 32, 64, 128)
+
+
+def pick_fastest(candidates, time_fn, repeats=3):
+    """The candidate with the least median of ``repeats`` timings
+    (``time_fn(c)`` returns seconds); ties go to the earlier candidate."""
+    best, best_t = None, None
+    for c in candidates:
+        ts = sorted(time_fn(c) for _ in range(repeats))
+        t = ts[len(ts) // 2]
+        if best_t is None or t < best_t:
+            best, best_t = c, t
+    return best
+
+
+class TuneCache:
+    """Tuned values per key, in memory and in a JSON file (read once,
+    rewritten after each new entry).  A file that cannot be read or written
+    only costs a re-tuning; the path is TRANSIFLOW_GB300_TUNE_CACHE, else
+    ~/.cache/transiflow_gb300/tune.json."""
+
+    def __init__(self, path=None):
+        self.path = path or os.environ.get('TRANSIFLOW_GB300_TUNE_CACHE') or os.path.join(
+            os.path.expanduser('~'), '.cache', 'transiflow_gb300', 'tune.json')
+        self.lock = threading.Lock()
+        self.data = None
+
+    def _load(self):
+        if self.data is None:
+            try:
+                with open(self.path) as f:
+                    d = json.load(f)
+                self.data = d if isinstance(d, dict) else {}
+            except (OSError, ValueError):
+                self.data = {}
+
+    def get(self, key):
+        with self.lock:
+            self._load()
+            return self.data.get(key)
+
+    def put(self, key, value):
+        with self.lock:
+            self._load()
+            self.data[key] = value
+            try:
+                os.makedirs(os.path.dirname(self.path) or '.', exist_ok=True)
+                tmp = self.path + '.%d.tmp' % os.getpid()
+                with open(tmp, 'w') as f:
+                    json.dump(self.data, f, indent=1, sort_keys=True)
+                os.replace(tmp, self.path)
+            except OSError:
+                pass
+
+
+_TUNE_CACHE = TuneCache()
 
 
 class _Engine:
@@ -331,12 +396,39 @@ class _Engine:
 
         self.solve_raw = solve
         self.lib = lib
+        # FP32 / BF16 per-height applications have a launch shape to tune
+        self.tuned = f64 or not solver.inverse or self.flow is not None
         if graphs:
             self.factor = _Graphed(factor, solver.stats)
             self.solve = _Graphed(solve, solver.stats)
         else:
             self.factor, self.solve = factor, solve
 
+
+    def tune(self, key, cache):
+        """Time the FP32 / BF16 application (on the factors just computed)
+        for each APPLY_WAVES target, keep the fastest in this engine's plan
+        descriptor and in the cache.  Runs before any CUDA graph holds an
+        application, so every later capture uses the tuned launches."""
+        self.tuned = True
+        best = cache.get(key)
+        if best not in APPLY_WAVES:
+            lib = self.lib
+            _lib.check(lib.tf_vec_fill(self.vec.numel(), 1.0, self.vec.data_ptr(), _stream()), 'tf_vec_fill')
+
+            def timed(w):
+                self.struct.apply_waves = w
+                self.solve_raw()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                self.solve_raw()
+                e1.record()
+                e1.synchronize()
+                return e0.elapsed_time(e1) / 1000.0
+            best = pick_fastest(APPLY_WAVES, timed)
+            cache.put(key, best)
+        self.struct.apply_waves = best
 
     def check(self):
         """Raises when a bounded wait of the dataflow application gave up
@@ -356,8 +448,11 @@ class Solver:
     def __init__(self, interface, restart=50, tol=1e-12, maxit=500, precision='fp64', reuse=True,
                  reuse_maxit=20, graphs=True, reuse_policy='cost', reuse_drift=0.05, inverse=True, flow=False,
                  flow_fuse_tiles=48, flow_chunk_tiles=24, leaf_cells=48, tc_min_front=1024,
-                 tc_terms=3, storage='fp32', inner='fp64', equilibrate=True, bordered='krylov'):
+                 tc_terms=3, storage='fp32', inner='fp64', equilibrate=True, bordered='krylov', tune=True):
         self.itf = interface
+        # FP32 / BF16 factors: time the application's launch shapes once per
+        # GPU, grid and precision (cached) and keep the fastest
+        self.tune = bool(tune)
         # bordered systems: one FGMRES on the bordered matrix, or block
         # elimination with two solves of the gauged Jacobian
         if bordered not in ('krylov', 'elimination'):
@@ -462,6 +557,11 @@ class Solver:
             eng = _Engine(self, precision, self.graphs)
             self._engines[precision] = eng
         return eng
+
+    def _tune_key(self, precision):
+        itf = self.itf
+        return '%s|%dx%dx%d|dof%d|%s|%s|apply_waves' % (torch.cuda.get_device_name(itf.device), itf.nx, itf.ny,
+                                                        itf.nz, itf.dof, precision, self.storage)
 
     def operator(self, jac):
         self._ensure_plan(jac.pattern)
