@@ -151,6 +151,33 @@ def test_quadratic_extrapolation_is_exact_on_a_parabola():
             assert torch.allclose(pred, x(sk + ds), rtol=0, atol=1e-12), (k, ds)
 
 
+def test_regular_steps_keep_what_the_history_describes():
+    """regular_steps keeps the samples whose quadratic extrapolation beats the
+    secant predictor -- here steps along a parabola, where it is exact -- and
+    drops the first step of a branch (no history) and a step whose history
+    points the wrong way."""
+    from transiflow_gb300.surrogate import _History, regular_steps
+    g = torch.Generator().manual_seed(7)
+    a, b, c = (torch.randn(6, dtype=torch.float64, generator=g) for _ in range(3))
+
+    def x(s):
+        return a + b * s + c * s * s
+    s_pts = [0.0, 0.5, 1.2, 1.8, 2.9]
+    hist = _History()
+    samples = []
+    t = b.clone()
+    for k in range(len(s_pts) - 1):
+        if k > 0:
+            t = (x(s_pts[k]) - x(s_pts[k - 1])) / (s_pts[k] - s_pts[k - 1])
+        p = hist.step(t, s_pts[k], 1.0)
+        ds = s_pts[k + 1] - s_pts[k]
+        samples.append({'x0': x(s_pts[k]), 't': t, 'p': p, 'phi': hist.phi(ds), 'ds': ds, 'x1': x(s_pts[k + 1]),
+                        'mu': s_pts[k]})
+    bad = dict(samples[-1], p=-50.0 * samples[-1]['p'])
+    kept = regular_steps(samples + [bad])
+    assert [s['mu'] for s in kept] == [s['mu'] for s in samples[1:]]
+
+
 def test_step_proposal_from_the_error_ratio():
     """The proposed step stretches ds by ratio^(-1/3) (the learned error,
     of third order in the step, then equals the secant error at ds), never

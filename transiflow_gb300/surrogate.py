@@ -165,7 +165,7 @@ def regular_steps(samples):
         xs = smp['x0'] + smp['ds'] * smp['t']
         es = float((smp['x1'] - xs).pow(2).mean().sqrt())
         eq = float((smp['x1'] - xs - (smp['ds'] ** 2 * phi) * p).pow(2).mean().sqrt())
-        if 0 < eq < es:
+        if eq < es:
             out.append(smp)
     return out
 
