@@ -6,13 +6,15 @@ top), Newton at Re = 0 from the zero state, then pseudo-arclength
 continuation in the Reynolds number from 0 to 2000 with ds = 100, every
 accepted point at ||F|| <= 1e-8.  Two arms on the same GPU:
 
-  learned+mixed  the learned continuation predictor (a 4-layer 3D CNN with 32
-                 channels, BF16 weights, FP32 accumulation), the secant
-                 predictor as fallback, FP32 multifrontal factors with
-                 tensor-core trailing updates as the preconditioner of FP64
-                 flexible GMRES to 1e-10 (the residual, the Newton update and
-                 the arclength scalars in FP64).  One step = one complete
-                 branch; `value` is the mean over the timed steps.
+  learned+mixed  the learned continuation predictor (three-point quadratic
+                 extrapolation plus a residual from a 4-layer 3D CNN with 32
+                 channels, BF16 weights, FP32 accumulation, used while it
+                 clearly beats the secant predictor), FP32 multifrontal
+                 factors with tensor-core trailing updates as the
+                 preconditioner of FP64 flexible GMRES to 1e-10 (the
+                 residual, the Newton update and the arclength scalars in
+                 FP64).  One step = one complete branch; `value` is the mean
+                 over the timed steps.
   plain FP64     the secant predictor and FP64 factors; run once per bench
                  invocation and reported beside the learned arm.
 
@@ -27,7 +29,10 @@ larger than L2, so no flush is needed between steps.
   e2e        the same steps through the public API: the start state copied
              from pinned host memory and the final state read back inside the
              timed region
-  roofline   the dominant kernel of the learned+mixed branch, timed live
+  roofline   the dominant step of the learned+mixed branch, one FP32
+             preconditioner application (HBM-bound), timed live, with the
+             factorisation, the tensor-core update, the assembly and the SpMV
+             beside it
   cpu_baseline  the oracle's CPU rhs / jacobian (a restatement of the
              reference's discretisation) on this host, sampled at 32^3 and
              scaled by the cell count, times the plain branch's call counts;
