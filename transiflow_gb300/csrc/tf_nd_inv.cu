@@ -426,26 +426,14 @@ static int factor_invert(const tf_nd_plan *p, const double *vals, T *fronts, int
 }
 
 // ---------------------------------------------------------------------------
-// Application with the inverted blocks.  Per height, two launches per sweep:
+// Application with inverted FP64 blocks (FP32 and BF16 factors: apply_kernel
+// further down).  Per height, two launches per sweep:
 //   forward   y = s + L11^-1 s into the scratch (s: the front's own rows of x
 //             in pivot order, gathered by each CTA), then x[bnd] -= L21 y;
 //   backward  t = y - U12 x[bnd] in the scratch, then x[own] = U11^-1 t.
 // x's own rows are written only by the backward product, so no launch reads
 // rows another CTA of the same launch writes.
 // ---------------------------------------------------------------------------
-// Factors may be stored in a narrower type than the one the products run in:
-// BF16 storage (converted from the FP32 factorisation) is applied in FP32.
-template <typename S>
-struct Arith {
-    using type = S;
-};
-template <>
-struct Arith<__nv_bfloat16> {
-    using type = float;
-};
-__device__ __forceinline__ float widen(__nv_bfloat16 v) { return __bfloat162float(v); }
-__device__ __forceinline__ float widen(float v) { return v; }
-__device__ __forceinline__ double widen(double v) { return v; }
 
 constexpr int VT = 128;            // rows (one thread each) per CTA of the row kernel
 constexpr int VW = 8;              // rows (one warp each) per CTA of the warp kernel
@@ -457,7 +445,7 @@ constexpr int VW = 8;              // rows (one warp each) per CTA of the warp k
 template <typename S, bool FWD>
 __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0, const S *fronts,
                                                             const int32_t *piv, double *x, double *packed) {
-    using T = typename Arith<S>::type;
+    using T = S;
     extern __shared__ double s_gather[];   // forward: s[0 .. rmax), then their indices in x
     pdl_trigger();
     const int node = node0 + blockIdx.y;
@@ -499,10 +487,10 @@ __global__ void __launch_bounds__(32 * VW) inv_apply_kernel(DevPlan P, int node0
     int c = c0 + lane;
 #pragma unroll 4
     for (; c + 32 < c1; c += 64) {
-        s0 += (T)widen(row[c]) * (T)sv[c];
-        s1 += (T)widen(row[c + 32]) * (T)sv[c + 32];
+        s0 += row[c] * (T)sv[c];
+        s1 += row[c + 32] * (T)sv[c + 32];
     }
-    if (c < c1) s0 += (T)widen(row[c]) * (T)sv[c];
+    if (c < c1) s0 += row[c] * (T)sv[c];
     T s = s0 + s1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
